@@ -1,0 +1,128 @@
+"""Seeded synthetic meshes in the reference's prepared-mesh form.
+
+* :func:`square_2d`  unit square, n x n quads each cut into 2 CST triangles,
+  left edge clamped (code 3), uniform traction on the right edge.
+* :func:`box_3d`     lx x ly x lz box of nx x ny x nz hexes, each cut into 6
+  Kuhn tetrahedra sharing the v000-v111 diagonal (conforming), interior nodes
+  jittered by U(-j h, +j h) per axis, face z=0 clamped (code 7), a uniform
+  traction on face z=lz and/or a point load.
+
+Nodes are lexicographic (i fastest, then j, then k). Coordinates are rounded
+to float32 so that the FP32 reference and the FP64 paths see the same
+geometry. Tractions are written as ``stress.txt`` rows whose "normal" is the
+traction direction and whose pressure is ``-|t|``, so that the reference's
+face-load formula (-coeff * p * L * n, cpu_fem_utils.cpp:564-582) pushes along
+the traction direction.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .meshio import Problem
+
+# Kuhn split of a hex with corners v0..v7 = (000,100,110,010,001,101,111,011) (dx,dy,dz)
+_HEX_CORNERS = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0],
+                         [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]], dtype=np.int64)
+_KUHN = np.array([[0, 1, 2, 6], [0, 2, 3, 6], [0, 3, 7, 6],
+                  [0, 7, 4, 6], [0, 4, 5, 6], [0, 5, 1, 6]], dtype=np.int64)
+_TET_FACES = np.array([[1, 2, 3, 0], [0, 2, 3, 1], [0, 1, 3, 2], [0, 1, 2, 3]])  # 3 face verts, opposite
+_TRI_EDGES = np.array([[1, 2, 0], [0, 2, 1], [0, 1, 2]])
+
+
+def _f32(a):
+    return np.asarray(a, dtype=np.float64).astype(np.float32).astype(np.float64)
+
+
+def square_2d(n: int = 64, E: float = 2e7, nu: float = 0.25, traction: float = 1e3) -> Problem:
+    """Unit square, n x n quads x 2 CST (config: 8192 elements at n=64)."""
+    xs = np.linspace(0.0, 1.0, n + 1)
+    X, Y = np.meshgrid(xs, xs, indexing="xy")        # node id = i + (n+1) j
+    nodes = _f32(np.stack([X.ravel(), Y.ravel()], axis=1))
+    nid = lambda i, j: i + (n + 1) * j
+    I, J = np.meshgrid(np.arange(n), np.arange(n), indexing="xy")
+    I, J = I.ravel(), J.ravel()
+    v00, v10, v11, v01 = nid(I, J), nid(I + 1, J), nid(I + 1, J + 1), nid(I, J + 1)
+    elems = np.empty((2 * n * n, 3), dtype=np.int32)
+    elems[0::2] = np.stack([v00, v10, v11], axis=1)
+    elems[1::2] = np.stack([v00, v11, v01], axis=1)
+    left = np.where(np.isclose(nodes[:, 0], 0.0))[0]
+    cons = np.stack([left, np.full_like(left, 3)], axis=1).astype(np.int32)
+    fn, fe = _boundary_faces(elems, nodes[:, 0] >= 1.0 - 1e-12)
+    F = len(fe)
+    return Problem(dim=2, nodes=nodes, elems=elems, cons=cons,
+                   load_node=np.zeros(0, np.int32), load_vec=np.zeros((0, 2)),
+                   face_nodes=fn, face_elem=fe, face_normal=np.tile([1.0, 0.0], (F, 1)),
+                   face_pressure=np.full(F, -abs(traction)), E=E, nu=nu)
+
+
+def _boundary_faces(elems: np.ndarray, on_plane: np.ndarray):
+    """Faces (edges in 2D) whose nodes all satisfy ``on_plane``; returns
+    ([F, dim+1] face nodes + opposite node, [F] element ids) in element order."""
+    nv = elems.shape[1]
+    tab = _TRI_EDGES if nv == 3 else _TET_FACES
+    rows, owners = [], []
+    for f in range(tab.shape[0]):
+        fv = elems[:, tab[f, :nv - 1]]
+        hit = np.all(on_plane[fv], axis=1)
+        idx = np.where(hit)[0]
+        rows.append(np.concatenate([fv[idx], elems[idx, tab[f, nv - 1]][:, None]], axis=1))
+        owners.append(idx)
+    rows = np.concatenate(rows, axis=0)
+    owners = np.concatenate(owners)
+    order = np.argsort(owners, kind="stable")
+    return rows[order].astype(np.int32), owners[order].astype(np.int32)
+
+
+def box_3d(nx: int, ny: int, nz: int, lx: float = 1.0, ly: float = 1.0, lz: float = 4.0,
+           jitter: float = 0.0, seed: int = 0, E: float = 2e7, nu: float = 0.25, rho: float = 2000.0,
+           traction=(0.0, -1e3, 0.0), point_load=None, clamp_code: int = 7) -> Problem:
+    """Kuhn-split tet box; face z=0 clamped, traction on z=lz, optional point load
+    ``point_load=(node_id or 'top_centre', (fx, fy, fz))``."""
+    h = np.array([lx / nx, ly / ny, lz / nz])
+    gi, gj, gk = np.meshgrid(np.arange(nx + 1), np.arange(ny + 1), np.arange(nz + 1), indexing="ij")
+    # lexicographic with i fastest: flatten in (k, j, i) order
+    gi, gj, gk = (a.transpose(2, 1, 0).ravel() for a in (gi, gj, gk))
+    nodes = np.stack([gi * h[0], gj * h[1], gk * h[2]], axis=1)
+    if jitter > 0:
+        rng = np.random.default_rng(seed)
+        d = rng.uniform(-jitter, jitter, size=nodes.shape) * h
+        interior = (gi > 0) & (gi < nx) & (gj > 0) & (gj < ny) & (gk > 0) & (gk < nz)
+        nodes[interior] += d[interior]
+    nodes = _f32(nodes)
+    nid = lambda i, j, k: i + (nx + 1) * (j + (ny + 1) * k)
+    HI, HJ, HK = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    HI, HJ, HK = (a.transpose(2, 1, 0).ravel() for a in (HI, HJ, HK))
+    corner = np.stack([nid(HI + c[0], HJ + c[1], HK + c[2]) for c in _HEX_CORNERS], axis=1)
+    elems = corner[:, _KUHN].reshape(-1, 4).astype(np.int32)
+    base = np.where(gk == 0)[0]
+    cons = np.stack([base, np.full_like(base, clamp_code)], axis=1).astype(np.int32)
+    fn = np.zeros((0, 4), np.int32)
+    fe = np.zeros(0, np.int32)
+    normals = np.zeros((0, 3))
+    press = np.zeros(0)
+    t = np.asarray(traction, dtype=np.float64) if traction is not None else np.zeros(3)
+    tmag = float(np.linalg.norm(t))
+    if tmag > 0:
+        fn, fe = _boundary_faces(elems, gk == nz)
+        normals = np.tile(t / tmag, (len(fe), 1))
+        press = np.full(len(fe), -tmag)
+    load_node = np.zeros(0, np.int32)
+    load_vec = np.zeros((0, 3))
+    if point_load is not None:
+        node, vec = point_load
+        if node == "top_centre":
+            node = nid(nx // 2, ny // 2, nz)
+        load_node = np.array([node], np.int32)
+        load_vec = _f32(np.asarray(vec, dtype=np.float64)[None, :])
+    return Problem(dim=3, nodes=nodes, elems=elems, cons=cons, load_node=load_node, load_vec=load_vec,
+                   face_nodes=fn, face_elem=fe, face_normal=normals, face_pressure=press,
+                   E=E, nu=nu, rho=rho)
+
+
+def cantilever_1p39m(seed: int = 0) -> Problem:
+    """1x1x4 box, 48x48x192 hexes x 6 tets (2,654,208 tets, 1,390,179 DOF), jitter 0.2h."""
+    return box_3d(48, 48, 192, jitter=0.2, seed=seed, traction=(0.0, -1e3, 0.0))
+
+
+def elem_centroid_z(p: Problem) -> np.ndarray:
+    return p.nodes[p.elems, 2].mean(axis=1)

@@ -1,0 +1,151 @@
+"""Regenerates the golden fixtures in tests/golden/ (run in a container that has
+the reference checkout; the GPU tests only read the committed outputs).
+
+    python tests/golden/make_golden.py [--ref /root/reference]
+
+1. The reference's own LS-DYNA parser (mesh_parser_lib/fem_parser.py) turns
+   raw_meshes/2D/{test_rect_pcg,9task_3}.k into prepared meshes (the committed
+   testing/*_mesh/stress.txt is in an older 6-column format the current reader
+   cannot parse). The displacement block of the reference's committed
+   testing/<task>_test/results.vtk is stored beside them.
+2. The reference's CPU path (oracle/_ref/ref_driver, built by oracle/ref.mk)
+   is run on those meshes and on small seeded synthetic meshes; its float32
+   outputs (static displacements, dynamics displacements and setup arrays)
+   are stored as .npz.
+"""
+from __future__ import annotations
+
+import argparse
+import contextlib
+import io
+import json
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+from cudafemproject_gb300 import meshgen, meshio  # noqa: E402
+
+DRIVER = os.path.join(REPO, "oracle", "_ref", "ref_driver")
+
+# Synthetic cases, small enough for the reference's O(n_e * n_c) setup.
+CASES = {
+    "sq8": dict(kind="2d", n=8),
+    "sq16": dict(kind="2d", n=16),
+    "box3": dict(kind="3d", n=(3, 3, 12), jitter=0.2, seed=0),
+    "box4p": dict(kind="3d", n=(4, 4, 8), jitter=0.15, seed=7, point=True),
+}
+DYN_CASES = {
+    # explicit central difference (beta2 = 0), jittered so element masses differ
+    "dyn_expl": dict(base="box3", rho=2000.0, beta1=0.5, beta2=0.0, dt=2e-5, endtime=2e-3,
+                     wavelet=dict(WaveletType="ricker", freq=25.0, timeshift=0.0, ampl=1.0)),
+    # implicit GN22 / Newmark (beta1 = 0.5, beta2 = 0.5)
+    "dyn_impl": dict(base="box3", rho=2000.0, beta1=0.5, beta2=0.5, dt=1e-3, endtime=2e-2,
+                     wavelet=dict(WaveletType="ricker", freq=25.0, timeshift=0.0, ampl=1.0)),
+    # explicit, Berlage wavelet, 2D
+    "dyn_expl2d": dict(base="sq8", rho=2000.0, beta1=0.5, beta2=0.0, dt=1e-5, endtime=1e-3,
+                       wavelet=dict(WaveletType="berlage", freq=15.0, timeshift=0.0, ampl=1.0)),
+}
+
+
+def make_problem(spec):
+    if spec["kind"] == "2d":
+        return meshgen.square_2d(spec["n"], E=2e7, nu=0.25, traction=1e3)
+    nx, ny, nz = spec["n"]
+    pl = ("top_centre", (0.0, 0.0, -1e3)) if spec.get("point") else None
+    return meshgen.box_3d(nx, ny, nz, jitter=spec["jitter"], seed=spec["seed"], E=2e7, nu=0.25,
+                          traction=(0.0, -1e3, 0.0), point_load=pl)
+
+
+def run_driver(mode, cfg_path, task, out):
+    res = subprocess.run([DRIVER, mode, cfg_path, task, out], check=True, capture_output=True, text=True)
+    return json.loads(res.stdout.strip().splitlines()[-1])
+
+
+def write_cfg(work, dim, E, nu, extra=None):
+    cfg = {"working_path": work, "DIM": dim, "youngModulus": E, "poissonRatio": nu}
+    cfg.update(extra or {})
+    path = os.path.join(work, "run_config.json")
+    with open(path, "w") as f:
+        json.dump(cfg, f)
+    return path
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    args = ap.parse_args()
+    if not os.path.exists(DRIVER):
+        subprocess.run(["make", "-f", "oracle/ref.mk", f"REF={args.ref}/FEMproject", "-j8"], cwd=REPO, check=True)
+    sys.path.insert(0, args.ref)
+    from mesh_parser_lib.fem_parser import run_parser  # the reference's own parser
+
+    meshes = os.path.join(HERE, "meshes")
+    # 1. reference fixtures
+    for task in ("test_rect_pcg", "9task_3"):
+        dst = os.path.join(meshes, "2D", task)
+        os.makedirs(dst, exist_ok=True)
+        with contextlib.redirect_stdout(io.StringIO()):
+            run_parser(args.ref + "/", dst, os.path.join(args.ref, "raw_meshes", "2D", task + ".k"), task, 2)
+        ref_vtk = os.path.join(args.ref, "testing", f"{task}_test", "results.vtk")
+        u = meshio.read_vtk_displacements(ref_vtk, 2)
+        np.savetxt(os.path.join(HERE, f"{task}_vtk_displacements.txt"), u, fmt="%.6g",
+                   header=f"displacements block of testing/{task}_test/results.vtk (reference fixture)")
+        with tempfile.TemporaryDirectory() as work:
+            shutil.copytree(os.path.join(meshes, "2D"), os.path.join(work, "prepared_meshes", "2D"))
+            cfg = write_cfg(work, 2, 2e7, 0.25)
+            out = os.path.join(work, "u.bin")
+            info = run_driver("static", cfg, task, out)
+            uref = np.fromfile(out, dtype=np.float32).reshape(-1, 2)
+            np.savez(os.path.join(HERE, f"ref_static_{task}.npz"), u=uref, iterations=info["pcg_iterations"])
+
+    # 2. synthetic cases
+    for name, spec in CASES.items():
+        p = make_problem(spec)
+        d = p.dim
+        dst = os.path.join(meshes, f"{d}D", name)
+        meshio.write_task(p, dst)
+        with tempfile.TemporaryDirectory() as work:
+            shutil.copytree(os.path.join(meshes, f"{d}D"), os.path.join(work, "prepared_meshes", f"{d}D"))
+            cfg = write_cfg(work, d, p.E, p.nu)
+            out = os.path.join(work, "u.bin")
+            info = run_driver("static", cfg, name, out)
+            u = np.fromfile(out, dtype=np.float32).reshape(-1, d)
+            os.makedirs(os.path.join(work, "dump"))
+            run_driver("dump", cfg, name, os.path.join(work, "dump"))
+            rd = lambda f: np.fromfile(os.path.join(work, "dump", f), dtype=np.float32)
+            extra = {}
+            if p.n_elems <= 2000:
+                extra["Klocals"] = rd("Klocals.bin")
+            np.savez_compressed(os.path.join(HERE, f"ref_static_{name}.npz"), u=u, iterations=info["pcg_iterations"],
+                                mask=rd("mask.bin"), adjElements=rd("adjElements.bin"), diagK=rd("diagK.bin"),
+                                Flocals=rd("Flocals.bin"), areas=rd("elementsAreas.bin"),
+                                constraintsIds=rd("constraintsIds.bin"), **extra)
+    for name, spec in DYN_CASES.items():
+        base = CASES[spec["base"]]
+        p = make_problem(base)
+        d = p.dim
+        with tempfile.TemporaryDirectory() as work:
+            shutil.copytree(os.path.join(meshes, f"{d}D"), os.path.join(work, "prepared_meshes", f"{d}D"))
+            extra = dict(task_type="dynamic", rho=spec["rho"], beta1=spec["beta1"], beta2=spec["beta2"],
+                         dt=spec["dt"], endtime=spec["endtime"], damping_alpha=0.0, damping_beta=0.0,
+                         wavelet=spec["wavelet"])
+            cfg = write_cfg(work, d, p.E, p.nu, extra)
+            out = os.path.join(work, "u.bin")
+            info = run_driver("dyn", cfg, spec["base"], out)
+            u = np.fromfile(out, dtype=np.float32).reshape(-1, d)
+            np.savez(os.path.join(HERE, f"ref_{name}.npz"), u=u, pcg_iterations=info["pcg_iterations"],
+                     **{k: v for k, v in spec.items() if k not in ("base", "wavelet")},
+                     base=spec["base"], wavelet=json.dumps(spec["wavelet"]))
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()
