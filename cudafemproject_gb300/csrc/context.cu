@@ -1,0 +1,766 @@
+// C-ABI implementation (include/cfem.h): context lifetime, static solvers.
+//
+// Host orchestration only; the arithmetic lives in kernels.cuh / kernels_aux.cuh.
+// PCG iterations are issued as captured CUDA graphs of 2*chunk kernels
+// (matvec with fused direction update, then the vector update), replayed until
+// the device-side stopping flag is set; all scalar recurrences stay on the GPU.
+#include "context_internal.cuh"
+#include "kernels_aux.cuh"
+
+namespace cfem {
+namespace detail {
+
+thread_local std::string g_last_error;
+
+template <typename T>
+MvParams<T> base_mv_t(cfem_ctx *c) {
+  MvParams<T> P{};
+  P.n_patches = c->prep.n_patches;
+  P.elem_off = c->elem_off.p;
+  P.node_off = c->node_off.p;
+  P.nodes = c->nodes.p;
+  P.own = c->own.p;
+  P.lconn = c->lconn.p;
+  P.bits = c->bits.p;
+  if constexpr (sizeof(T) == 8) P.G = c->G64.p; else P.G = c->G32.p;
+  P.gstride = c->gstride;
+  P.mcoef = nullptr;
+  P.lam = (T)c->lam;
+  P.mu = (T)c->mu;
+  P.cK = 1;
+  P.cM = 0;
+  P.partials = c->partials.p;
+  return P;
+}
+
+template <typename T>
+void launch_mv_t(cfem_ctx *c, int mode, const MvParams<T> &P) {
+  size_t smem = sizeof(T) == 8 ? c->smem64 : c->smem32;
+  dim3 g(c->grid_mv), b(kThreads);
+  if (c->dim == 3) {
+    if (mode == MV_PLAIN) k_matvec<T, 3, MV_PLAIN><<<g, b, smem, c->stream>>>(P);
+    else if (mode == MV_PCG) k_matvec<T, 3, MV_PCG><<<g, b, smem, c->stream>>>(P);
+    else k_matvec<T, 3, MV_DYN><<<g, b, smem, c->stream>>>(P);
+  } else {
+    if (mode == MV_PLAIN) k_matvec<T, 2, MV_PLAIN><<<g, b, smem, c->stream>>>(P);
+    else if (mode == MV_PCG) k_matvec<T, 2, MV_PCG><<<g, b, smem, c->stream>>>(P);
+    else k_matvec<T, 2, MV_DYN><<<g, b, smem, c->stream>>>(P);
+  }
+  CKL();
+}
+
+template <typename T>
+VecParams<T> vec_params(cfem_ctx *c, Vecs<T> &V, T *p, Scalars *sc) {
+  VecParams<T> P{};
+  P.n_nodes = c->nn;
+  P.x = V.x.p; P.r = V.r.p; P.z = V.z.p; P.p = p; P.u = V.u.p;
+  P.dinv = V.dinv.p;
+  P.f = V.f.p;
+  P.sc = sc;
+  P.partials = c->partials.p;
+  return P;
+}
+
+template <typename T>
+void launch_init(cfem_ctx *c, const VecParams<T> &P, int warm) {
+  if (c->dim == 3) k_pcg_init<T, 3><<<c->grid_vec, kThreads, 0, c->stream>>>(P, warm);
+  else k_pcg_init<T, 2><<<c->grid_vec, kThreads, 0, c->stream>>>(P, warm);
+  CKL();
+}
+
+template <typename T>
+void launch_update(cfem_ctx *c, const VecParams<T> &P) {
+  if (c->dim == 3) k_pcg_update<T, 3><<<c->grid_vec, kThreads, 0, c->stream>>>(P);
+  else k_pcg_update<T, 2><<<c->grid_vec, kThreads, 0, c->stream>>>(P);
+  CKL();
+}
+
+// Jacobi PCG on A x = V.f with A = cM*M + cK*K' (mcoef selects the mass term).
+// V.x holds the warm start when warm != 0. Returns after the device flag says done.
+template <typename T>
+PcgResult run_pcg_t(cfem_ctx *c, Vecs<T> &V, T cK, T cM, const T *mcoef, int warm, double tol, int rule, int maxit) {
+  Scalars *sc = c->sc.p + (sizeof(T) == 8 ? 0 : 1);
+  Scalars h{};
+  h.tol = tol;
+  h.rule = rule;
+  h.maxit = maxit > 0 ? maxit : 1000000;
+  CK(cudaMemcpyAsync(sc, &h, sizeof(Scalars), cudaMemcpyHostToDevice, c->stream));
+  MvParams<T> mv = base_mv<T>(c);
+  mv.cK = cK;
+  mv.cM = cM;
+  mv.mcoef = mcoef;
+  mv.diagA = V.diagA.p;
+  mv.sc = sc;
+  if (warm) {
+    mv.x = V.x.p;
+    mv.y = V.u.p;
+    V.u.zero(c->stream);
+    launch_mv<T>(c, MV_PLAIN, mv);
+  }
+  launch_init<T>(c, vec_params<T>(c, V, V.pA.p, sc), warm);
+  GraphCache &gc = sizeof(T) == 8 ? c->graph64 : c->graph32;
+  if (!gc.exec || gc.key0 != (const void *)mcoef || gc.key1 != (double)cK || gc.key2 != (double)cM) {
+    gc.reset();
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    for (int it = 0; it < c->chunk; ++it) {
+      T *pold = (it & 1) ? V.pB.p : V.pA.p;
+      T *pnew = (it & 1) ? V.pA.p : V.pB.p;
+      MvParams<T> m = mv;
+      m.x = V.z.p;
+      m.x2 = pold;
+      m.xout = pnew;
+      m.y = V.u.p;
+      launch_mv<T>(c, MV_PCG, m);
+      launch_update<T>(c, vec_params<T>(c, V, pnew, sc));
+    }
+    CK(cudaStreamEndCapture(c->stream, &graph));
+    CK(cudaGraphInstantiate(&gc.exec, graph, 0));
+    cudaGraphDestroy(graph);
+    gc.key0 = mcoef;
+    gc.key1 = cK;
+    gc.key2 = cM;
+  }
+  PcgResult res;
+  // Every replay advances the iteration count by `chunk` unless the device
+  // flag is set; the cap below only guards against a stalled recurrence.
+  const int64_t max_launches = (int64_t)h.maxit / c->chunk + 16;
+  int last_iter = -1, stalled = 0;
+  for (int64_t launch = 0;; ++launch) {
+    if (launch > max_launches || stalled > 4)
+      throw Fail{CFEM_ERR_CUDA, "PCG recurrence stopped advancing on the device"};
+    CK(cudaGraphLaunch(gc.exec, c->stream));
+    CK(cudaMemcpyAsync(c->h_sc, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (c->verbose)
+      std::printf("iteration %d gamma %.6e gamma0 %.6e\n", c->h_sc->iter, c->h_sc->gamma, c->h_sc->gamma0);
+    if (c->h_sc->done) break;
+    stalled = c->h_sc->iter == last_iter ? stalled + 1 : 0;
+    last_iter = c->h_sc->iter;
+  }
+  res.iters = c->h_sc->iter;
+  res.gamma0 = c->h_sc->gamma0;
+  res.gamma = c->h_sc->gamma;
+  res.rr = c->h_sc->rr;
+  res.ff = c->h_sc->ff;
+  int d = c->h_sc->done;
+  res.status = d == 1 ? CFEM_OK : d == 2 ? CFEM_ERR_DIVERGED : CFEM_ERR_NOT_CONVERGED;
+  return res;
+}
+
+// caller-order FP64 array (host or device) -> internal node vector of type T
+template <typename T>
+void to_internal_t(cfem_ctx *c, const double *src, T *dst, double scale) {
+  CK(cudaMemcpyAsync(c->io.p, src, sizeof(double) * c->nd, cudaMemcpyDefault, c->stream));
+  if (c->dim == 3) k_to_internal<T, 3><<<nblk(c->nn), kThreads, 0, c->stream>>>(c->nn, c->io.p, c->node_new2old.p, dst, scale);
+  else k_to_internal<T, 2><<<nblk(c->nn), kThreads, 0, c->stream>>>(c->nn, c->io.p, c->node_new2old.p, dst, scale);
+  CKL();
+}
+
+template <typename T>
+void to_caller_t(cfem_ctx *c, const T *src, double *dst) {
+  if (c->dim == 3) k_to_caller<T, 3><<<nblk(c->nn), kThreads, 0, c->stream>>>(c->nn, src, c->node_new2old.p, c->io.p);
+  else k_to_caller<T, 2><<<nblk(c->nn), kThreads, 0, c->stream>>>(c->nn, src, c->node_new2old.p, c->io.p);
+  CKL();
+  CK(cudaMemcpyAsync(dst, c->io.p, sizeof(double) * c->nd, cudaMemcpyDefault, c->stream));
+}
+
+MvParams<double> base_mv_d(cfem_ctx *c) { return base_mv_t<double>(c); }
+MvParams<float> base_mv_f(cfem_ctx *c) { return base_mv_t<float>(c); }
+void launch_mv_d(cfem_ctx *c, int mode, const MvParams<double> &P) { launch_mv_t<double>(c, mode, P); }
+void launch_mv_f(cfem_ctx *c, int mode, const MvParams<float> &P) { launch_mv_t<float>(c, mode, P); }
+PcgResult run_pcg_d(cfem_ctx *c, Vecs<double> &V, double cK, double cM, const double *mcoef, int warm, double tol,
+                    int rule, int maxit) {
+  return run_pcg_t<double>(c, V, cK, cM, mcoef, warm, tol, rule, maxit);
+}
+PcgResult run_pcg_f(cfem_ctx *c, Vecs<float> &V, float cK, float cM, const float *mcoef, int warm, double tol,
+                    int rule, int maxit) {
+  return run_pcg_t<float>(c, V, cK, cM, mcoef, warm, tol, rule, maxit);
+}
+void to_internal_d(cfem_ctx *c, const double *src, double *dst, double scale) { to_internal_t<double>(c, src, dst, scale); }
+void to_internal_f(cfem_ctx *c, const double *src, float *dst, double scale) { to_internal_t<float>(c, src, dst, scale); }
+void to_caller_d(cfem_ctx *c, const double *src, double *dst) { to_caller_t<double>(c, src, dst); }
+void to_caller_f(cfem_ctx *c, const float *src, double *dst) { to_caller_t<float>(c, src, dst); }
+
+// FP64 true residual r = f - K' x (f, x internal FP64). Returns ||r||^2, ||f||^2.
+void true_residual(cfem_ctx *c, const double *f, const double *x, double *r, float *r32, double &rr, double &ff) {
+  MvParams<double> mv = base_mv<double>(c);
+  mv.diagA = c->diagK.p;
+  mv.x = x;
+  mv.y = c->tmp64.p;
+  c->tmp64.zero(c->stream);
+  launch_mv<double>(c, MV_PLAIN, mv);
+  ResParams P{};
+  P.nvec = c->nvec;
+  P.f = f;
+  P.u = c->tmp64.p;
+  P.r = r;
+  P.r32 = r32;
+  P.out = c->rr.p;
+  P.partials = c->partials.p;
+  P.count = c->counters.p;
+  k_residual<<<c->grid_vec, kThreads, 0, c->stream>>>(P);
+  CKL();
+  CK(cudaMemcpyAsync(c->h_rr, c->rr.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  rr = c->h_rr[0];
+  ff = c->h_rr[1];
+}
+
+void set_diag_vectors(cfem_ctx *c, const double *diagA64) {
+  // dinv and diagA for both precisions from one FP64 diagonal (internal layout)
+  k_invert<double><<<nblk(c->nvec), kThreads, 0, c->stream>>>(c->nvec, diagA64, c->v64.dinv.p);
+  k_invert<float><<<nblk(c->nvec), kThreads, 0, c->stream>>>(c->nvec, diagA64, c->v32.dinv.p);
+  CK(cudaMemcpyAsync(c->v64.diagA.p, diagA64, sizeof(double) * c->nvec, cudaMemcpyDeviceToDevice, c->stream));
+  k_convert<double, float><<<nblk(c->nvec), kThreads, 0, c->stream>>>(c->nvec, diagA64, c->v32.diagA.p);
+  CKL();
+}
+
+// Static-type solve of K' x = f (f internal FP64 in c->v64.f). Result in c->v64.x.
+cfem_status solve_internal(cfem_ctx *c, const cfem_solve_params *prm, cfem_solve_info *info) {
+  cfem_solve_info inf{};
+  set_diag_vectors(c, c->diagK.p);
+  CK(cudaEventRecord(c->ev0, c->stream));
+  const int prec = prm->precision;
+  int status = CFEM_OK;
+  if (prec == CFEM_FP64) {
+    PcgResult r = run_pcg<double>(c, c->v64, 1.0, 0.0, nullptr, 0, prm->tol, prm->stop_rule, prm->max_iter);
+    status = r.status;
+    inf.iterations = r.iters;
+    inf.gamma0 = r.gamma0;
+    inf.gamma = r.gamma;
+  } else if (prec == CFEM_FP32) {
+    k_convert<double, float><<<nblk(c->nvec), kThreads, 0, c->stream>>>(c->nvec, c->v64.f.p, c->v32.f.p);
+    CKL();
+    PcgResult r = run_pcg<float>(c, c->v32, 1.f, 0.f, nullptr, 0, prm->tol, prm->stop_rule, prm->max_iter);
+    status = r.status;
+    inf.iterations = r.iters;
+    inf.gamma0 = r.gamma0;
+    inf.gamma = r.gamma;
+    k_convert<float, double><<<nblk(c->nvec), kThreads, 0, c->stream>>>(c->nvec, c->v32.x.p, c->v64.x.p);
+    CKL();
+  } else if (prec == CFEM_FP32_REFINE) {
+    // x64 = 0; r64 = f; repeat: solve K d = r (FP32), x64 += d, r64 = f - K64 x64
+    c->v64.x.zero(c->stream);
+    double rr = 0, ff = 0;
+    true_residual(c, c->v64.f.p, c->v64.x.p, c->v64.r.p, c->v32.f.p, rr, ff);
+    const double outer_tol = prm->outer_tol > 0 ? prm->outer_tol : 1e-12;
+    const int max_outer = prm->max_outer > 0 ? prm->max_outer : 50;
+    int outer = 0, total = 0;
+    status = CFEM_ERR_NOT_CONVERGED;
+    while (outer < max_outer) {
+      if (std::sqrt(rr) <= outer_tol * std::sqrt(ff)) { status = CFEM_OK; break; }
+      PcgResult r = run_pcg<float>(c, c->v32, 1.f, 0.f, nullptr, 0, prm->tol, prm->stop_rule, prm->max_iter);
+      total += r.iters;
+      if (outer == 0) inf.gamma0 = r.gamma0;
+      inf.gamma = r.gamma;
+      if (r.status == CFEM_ERR_DIVERGED) { status = CFEM_ERR_DIVERGED; break; }
+      k_accumulate<<<nblk(c->nvec), kThreads, 0, c->stream>>>(c->nvec, c->v32.x.p, c->v64.x.p);
+      CKL();
+      ++outer;
+      true_residual(c, c->v64.f.p, c->v64.x.p, c->v64.r.p, c->v32.f.p, rr, ff);
+    }
+    if (status != CFEM_OK && std::sqrt(rr) <= outer_tol * std::sqrt(ff)) status = CFEM_OK;
+    inf.iterations = total;
+    inf.outer_iterations = outer;
+  } else {
+    throw Fail{CFEM_ERR_INVALID_ARGUMENT, "unknown precision"};
+  }
+  CK(cudaEventRecord(c->ev1, c->stream));
+  CK(cudaEventSynchronize(c->ev1));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  inf.solve_ms = ms;
+  double rr = 0, ff = 0;
+  true_residual(c, c->v64.f.p, c->v64.x.p, c->tmp64b.p, nullptr, rr, ff);
+  inf.rel_residual = ff > 0 ? std::sqrt(rr / ff) : std::sqrt(rr);
+  inf.status = status;
+  if (info) *info = inf;
+  return (cfem_status)status;
+}
+
+// F(t) = a FA + b FB into the internal FP64 vector dst
+void make_rhs(cfem_ctx *c, double a, double b, double *dst) {
+  CK(cudaMemsetAsync(dst, 0, sizeof(double) * c->nvec, c->stream));
+  if (a != 0) k_axpby64<<<nblk(c->nvec), kThreads, 0, c->stream>>>(c->nvec, a, c->FA.p, 1.0, dst);
+  if (b != 0) k_axpby64<<<nblk(c->nvec), kThreads, 0, c->stream>>>(c->nvec, b, c->FB.p, 1.0, dst);
+  CKL();
+}
+
+// ======================================================================== C-ABI
+cfem_status run_guarded(const std::function<cfem_status()> &fn) {
+  try {
+    return fn();
+  } catch (const Fail &f) {
+    g_last_error = f.msg;
+    return f.st;
+  } catch (const std::bad_alloc &) {
+    g_last_error = "host out of memory";
+    return CFEM_ERR_OUT_OF_MEMORY;
+  } catch (const std::exception &e) {
+    g_last_error = e.what();
+    return CFEM_ERR_INVALID_ARGUMENT;
+  }
+}
+
+void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, const cfem_options *opt) {
+  c->dim = m->dim;
+  c->nv = m->dim + 1;
+  c->w = 6 * (m->dim - 1);
+  c->vw = m->dim == 3 ? 4 : 2;
+  c->ncomp = m->dim * m->dim;
+  c->nn = m->n_nodes;
+  c->ne = m->n_elems;
+  c->nd = c->nn * c->dim;
+  c->nvec = c->nn * c->vw;
+  c->semantics = opt ? opt->semantics : CFEM_COMPAT;
+  c->form = CFEM_FORM_GRADIENT;
+  if (opt && opt->matvec_form == CFEM_FORM_STORED_KE)
+    throw Fail{CFEM_ERR_UNSUPPORTED, "stored K_e form is not built in this library version"};
+  c->verbose = opt ? opt->verbose : 0;
+  c->E = mat ? mat->young_modulus : 2e7;
+  c->nu = mat ? mat->poisson_ratio : 0.3;
+  c->rho = mat ? mat->rho : 2400.0;
+  if (!(c->E > 0) || !(c->nu > -1.0) || !(c->nu < 0.5)) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "invalid material"};
+  if (c->dim == 3) {
+    c->lam = c->E * c->nu / ((1 + c->nu) * (1 - 2 * c->nu));
+    c->mu = c->E / (2 * (1 + c->nu));
+  } else {  // plane stress (datakeeper.cpp:100-104)
+    c->lam = c->E * c->nu / (1 - c->nu * c->nu);
+    c->mu = c->E / (2 * (1 + c->nu));
+  }
+  CK(cudaGetDevice(&c->device));
+  CK(cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, c->device));
+  int pe = opt && opt->patch_elems > 0 ? opt->patch_elems : 512;
+  std::string err = build_prep(*m, pe, c->prep);
+  if (!err.empty()) throw Fail{CFEM_ERR_MESH, err};
+  err = build_rhs(*m, c->prep, c->semantics, c->rhs);
+  if (!err.empty()) throw Fail{CFEM_ERR_MESH, err};
+  c->elems_caller.assign(m->elems, m->elems + c->ne * c->nv);
+  if (m->elem_young) {
+    c->young.assign(m->elem_young, m->elem_young + c->ne);
+    for (double y : c->young)
+      if (!(y > 0)) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "per-element Young's modulus must be positive"};
+  }
+  const Prep &P = c->prep;
+  cudaStream_t s = c->stream;
+  c->elem_off.upload(P.p_elem_off.data(), P.p_elem_off.size(), s);
+  c->node_off.upload(P.p_node_off.data(), P.p_node_off.size(), s);
+  c->nodes.upload(P.p_nodes.data(), P.p_nodes.size(), s);
+  c->own.upload(P.p_own.data(), P.p_own.size(), s);
+  c->node_new2old.upload(P.node_new2old.data(), P.node_new2old.size(), s);
+  c->node_old2new.upload(P.node_old2new.data(), P.node_old2new.size(), s);
+  c->elem_new2old.upload(P.elem_new2old.data(), P.elem_new2old.size(), s);
+  c->elem_old2new.upload(P.elem_old2new.data(), P.elem_old2new.size(), s);
+  c->lconn.upload(reinterpret_cast<const uint2 *>(P.lconn.data()), (size_t)c->ne, s);
+  c->bits.upload(P.node_bits.data(), P.node_bits.size(), s);
+  // coordinates and global connectivity in the new order (setup + checks)
+  {
+    std::vector<double> xyz((size_t)c->nn * c->dim);
+    for (int64_t n = 0; n < c->nn; ++n)
+      for (int d = 0; d < c->dim; ++d) xyz[n * c->dim + d] = m->nodes[(int64_t)P.node_new2old[n] * c->dim + d];
+    c->coords.upload(xyz.data(), xyz.size(), s);
+    std::vector<int32_t> cn((size_t)c->ne * c->nv);
+    for (int64_t e = 0; e < c->ne; ++e)
+      for (int a = 0; a < c->nv; ++a)
+        cn[e * c->nv + a] = P.node_old2new[m->elems[(int64_t)P.elem_new2old[e] * c->nv + a]];
+    c->conn.upload(cn.data(), cn.size(), s);
+  }
+  rebuild_operator(c);
+  // right-hand side parts in the internal layout
+  c->io.alloc(c->nd);
+  c->FA.alloc(c->nvec);
+  c->FB.alloc(c->nvec);
+  c->FA32.alloc(c->nvec);
+  c->FB32.alloc(c->nvec);
+  c->v64.f.alloc(c->nvec);
+  // work vectors
+  for (auto *b : {&c->v64.x, &c->v64.r, &c->v64.z, &c->v64.pA, &c->v64.pB, &c->v64.u, &c->v64.dinv, &c->v64.diagA}) {
+    b->alloc(c->nvec);
+    b->zero(s);
+  }
+  c->v64.f.zero(s);
+  for (auto *b : {&c->v32.x, &c->v32.r, &c->v32.z, &c->v32.pA, &c->v32.pB, &c->v32.u, &c->v32.f, &c->v32.dinv, &c->v32.diagA}) {
+    b->alloc(c->nvec);
+    b->zero(s);
+  }
+  c->tmp64.alloc(c->nvec);
+  c->tmp64b.alloc(c->nvec);
+  c->tmp64.zero(s);
+  c->tmp64b.zero(s);
+  to_internal<double>(c, c->rhs.FA.data(), c->FA.p);
+  to_internal<double>(c, c->rhs.FB.data(), c->FB.p);
+  k_convert<double, float><<<nblk(c->nvec), kThreads, 0, s>>>(c->nvec, c->FA.p, c->FA32.p);
+  k_convert<double, float><<<nblk(c->nvec), kThreads, 0, s>>>(c->nvec, c->FB.p, c->FB32.p);
+  CKL();
+  // launch shapes
+  c->smem64 = (size_t)P.np_max * c->vw * 2 * sizeof(double);
+  c->smem32 = (size_t)P.np_max * c->vw * 2 * sizeof(float);
+  auto set_smem = [&](const void *k, size_t bytes) {
+    CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(bytes, 1)));
+  };
+  int occ = 1;
+  if (c->dim == 3) {
+    set_smem((const void *)k_matvec<double, 3, MV_PLAIN>, c->smem64);
+    set_smem((const void *)k_matvec<double, 3, MV_PCG>, c->smem64);
+    set_smem((const void *)k_matvec<double, 3, MV_DYN>, c->smem64);
+    set_smem((const void *)k_matvec<float, 3, MV_PLAIN>, c->smem32);
+    set_smem((const void *)k_matvec<float, 3, MV_PCG>, c->smem32);
+    set_smem((const void *)k_matvec<float, 3, MV_DYN>, c->smem32);
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_matvec<float, 3, MV_PCG>, kThreads, c->smem32));
+  } else {
+    set_smem((const void *)k_matvec<double, 2, MV_PLAIN>, c->smem64);
+    set_smem((const void *)k_matvec<double, 2, MV_PCG>, c->smem64);
+    set_smem((const void *)k_matvec<double, 2, MV_DYN>, c->smem64);
+    set_smem((const void *)k_matvec<float, 2, MV_PLAIN>, c->smem32);
+    set_smem((const void *)k_matvec<float, 2, MV_PCG>, c->smem32);
+    set_smem((const void *)k_matvec<float, 2, MV_DYN>, c->smem32);
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_matvec<float, 2, MV_PCG>, kThreads, c->smem32));
+  }
+  occ = std::max(occ, 1);
+  c->grid_mv = (int)std::min<int64_t>(P.n_patches, (int64_t)c->n_sm * occ);
+  c->grid_vec = (int)std::min<int64_t>(std::max<int64_t>(1, nblk(c->nn)), (int64_t)c->n_sm * 4);
+  int maxgrid = std::max(c->grid_mv, c->grid_vec);
+  c->partials.alloc((size_t)maxgrid * 4);
+  c->counters.alloc(4);
+  c->counters.zero(s);
+  c->rr.alloc(4);
+  c->sc.alloc(3);
+  c->sc.zero(s);
+  CK(cudaMallocHost(&c->h_sc, sizeof(Scalars)));
+  CK(cudaMallocHost(&c->h_rr, 4 * sizeof(double)));
+  CK(cudaEventCreate(&c->ev0));
+  CK(cudaEventCreate(&c->ev1));
+  CK(cudaStreamSynchronize(s));
+}
+
+// (Re)builds the element operator: scaled gradients, volumes, assembled
+// diagonal and masses (calculateKlocals / calculateMlocals equivalents).
+void rebuild_operator(cfem_ctx *c) {
+  cudaStream_t s = c->stream;
+  const Prep &P = c->prep;
+  (void)P;
+  if (!c->young.empty()) {
+    std::vector<double> sc(c->ne);
+    for (int64_t e = 0; e < c->ne; ++e) sc[e] = c->young[c->prep.elem_new2old[e]] / c->E;
+    c->escale.upload(sc.data(), sc.size(), s);
+    c->young_d.upload(c->young.data(), c->young.size(), s);
+  }
+  c->gstride = (c->ne + 31) / 32 * 32;
+  c->G64.alloc((size_t)c->ncomp * c->gstride);
+  c->G32.alloc((size_t)c->ncomp * c->gstride);
+  c->vol.alloc(c->ne);
+  c->mc64.alloc(c->ne);
+  c->mc32.alloc(c->ne);
+  c->diagK.alloc(c->nvec);
+  c->mlump.alloc(c->nvec);
+  c->mcdiag.alloc(c->nvec);
+  c->diagK.zero(s);
+  c->mlump.zero(s);
+  c->mcdiag.zero(s);
+  if (!c->err.p) c->err.alloc(1);
+  c->err.zero(s);
+  c->G64.zero(s);
+  c->G32.zero(s);
+  // mass factors: lumped per DOF and consistent coefficient (M_ab = c (1 + delta_ab) rho V)
+  double &lump_c = c->lump_c, &cons_c = c->cons_c;
+  if (c->dim == 2) { lump_c = 1.0 / 3; cons_c = 1.0 / 12; }
+  else if (c->semantics == CFEM_COMPAT) { lump_c = 1.0 / 12; cons_c = 1.0 / 48; }  // cpu_fem_utils.cpp:656-726
+  else { lump_c = 1.0 / 4; cons_c = 1.0 / 20; }
+  GeomParams gp{};
+  gp.ne = c->ne;
+  gp.gstride = c->gstride;
+  gp.coords = c->coords.p;
+  gp.conn = c->conn.p;
+  gp.escale = c->escale.p;
+  gp.lam = c->lam;
+  gp.mu = c->mu;
+  gp.rho = c->rho;
+  gp.lump_c = lump_c;
+  gp.cons_c = cons_c;
+  gp.G64 = c->G64.p;
+  gp.G32 = c->G32.p;
+  gp.vol = c->vol.p;
+  gp.diagK = c->diagK.p;
+  gp.mlump = c->mlump.p;
+  gp.mc64 = c->mc64.p;
+  gp.mc32 = c->mc32.p;
+  gp.diag_local = nullptr;
+  gp.elem_new2old = c->elem_new2old.p;
+  gp.err = c->err.p;
+  if (c->dim == 3) k_geometry<3><<<nblk(c->ne), kThreads, 0, s>>>(gp);
+  else k_geometry<2><<<nblk(c->ne), kThreads, 0, s>>>(gp);
+  CKL();
+  // consistent-mass diagonal: 2 * cons_c * rho * V per DOF, assembled = mlump * 2 cons_c / lump_c
+  k_axpby64<<<nblk(c->nvec), kThreads, 0, s>>>(c->nvec, 2 * cons_c / lump_c, c->mlump.p, 0.0, c->mcdiag.p);
+  CKL();
+  int herr = 0;
+  c->diagK32.alloc(c->nvec);
+  k_convert<double, float><<<nblk(c->nvec), kThreads, 0, s>>>(c->nvec, c->diagK.p, c->diagK32.p);
+  CKL();
+  CK(cudaMemcpyAsync(&herr, c->err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (herr) throw Fail{CFEM_ERR_MESH, "an element has zero or non-finite volume"};
+}
+
+void check_ctx(const cfem_ctx *c) {
+  if (!c) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "null context"};
+}
+
+cfem_solve_params default_params() {
+  cfem_solve_params p{};
+  p.precision = CFEM_FP64;
+  p.stop_rule = CFEM_STOP_REFERENCE;
+  p.tol = 1e-8;
+  p.max_iter = 1000000;
+  p.outer_tol = 1e-12;
+  p.max_outer = 50;
+  return p;
+}
+
+}  // namespace detail
+}  // namespace cfem
+
+extern "C" {
+
+int32_t cfem_abi_version(void) { return CFEM_ABI_VERSION; }
+
+const char *cfem_last_error_string(void) { return g_last_error.c_str(); }
+
+cfem_status cfem_create(cfem_ctx **out, const cfem_mesh *mesh, const cfem_material *mat, const cfem_options *opt,
+                        void *stream) {
+  return run_guarded([&]() -> cfem_status {
+    if (!out || !mesh) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "null argument"};
+    *out = nullptr;
+    if (!mesh->nodes || !mesh->elems) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "mesh without nodes or elements"};
+    if ((mesh->n_constraints > 0 && !mesh->constraints) || (mesh->n_loads > 0 && (!mesh->load_nodes || !mesh->load_vectors)) ||
+        (mesh->n_faces > 0 && (!mesh->face_nodes || !mesh->face_elems || !mesh->face_normals || !mesh->face_pressures)))
+      throw Fail{CFEM_ERR_INVALID_ARGUMENT, "mesh count given without its array"};
+    std::unique_ptr<cfem_ctx> c(new cfem_ctx());
+    c->stream = (cudaStream_t)stream;
+    setup_context(c.get(), mesh, mat, opt);
+    *out = c.release();
+    return CFEM_OK;
+  });
+}
+
+void cfem_destroy(cfem_ctx *ctx) {
+  if (!ctx) return;
+  cudaStreamSynchronize(ctx->stream);
+  delete ctx;
+}
+
+cfem_status cfem_set_stream(cfem_ctx *ctx, void *stream) {
+  return run_guarded([&]() -> cfem_status {
+    check_ctx(ctx);
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->stream = (cudaStream_t)stream;
+    ctx->graph64.reset();
+    ctx->graph32.reset();
+    return CFEM_OK;
+  });
+}
+
+cfem_status cfem_synchronize(cfem_ctx *ctx) {
+  return run_guarded([&]() -> cfem_status {
+    check_ctx(ctx);
+    CK(cudaStreamSynchronize(ctx->stream));
+    return CFEM_OK;
+  });
+}
+
+cfem_status cfem_get_counts(const cfem_ctx *ctx, int64_t *counts) {
+  return run_guarded([&]() -> cfem_status {
+    check_ctx(ctx);
+    if (!counts) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "null counts"};
+    counts[0] = ctx->dim; counts[1] = ctx->nn; counts[2] = ctx->ne; counts[3] = ctx->nd;
+    counts[4] = ctx->prep.n_patches; counts[5] = ctx->form;
+    return CFEM_OK;
+  });
+}
+
+cfem_status cfem_dof_map(const cfem_ctx *ctx, int32_t *mask) {
+  return run_guarded([&]() -> cfem_status {
+    check_ctx(ctx);
+    if (!mask) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "null mask"};
+    // element-local slot (caller element e, vertex a, component d) -> dim*node + d
+    const Prep &P = ctx->prep;
+    for (int64_t ei = 0; ei < ctx->ne; ++ei) {
+      int64_t e = P.elem_new2old[ei];
+      for (int a = 0; a < ctx->nv; ++a) {
+        int patch = (int)(ei / P.patch_elems);
+        int g = P.p_nodes[P.p_node_off[patch] + P.lconn[ei * 4 + a]];
+        int64_t node = P.node_new2old[g];
+        for (int d = 0; d < ctx->dim; ++d) mask[e * ctx->w + ctx->dim * a + d] = (int32_t)(ctx->dim * node + d);
+      }
+    }
+    return CFEM_OK;
+  });
+}
+
+cfem_status cfem_adjacency(const cfem_ctx *ctx, int32_t *adj) {
+  return run_guarded([&]() -> cfem_status {
+    check_ctx(ctx);
+    if (!adj) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "null adj"};
+    std::fill(adj, adj + ctx->nd, 0);
+    const Prep &P = ctx->prep;
+    for (int64_t ei = 0; ei < ctx->ne; ++ei) {
+      int patch = (int)(ei / P.patch_elems);
+      for (int a = 0; a < ctx->nv; ++a) {
+        int64_t node = P.node_new2old[P.p_nodes[P.p_node_off[patch] + P.lconn[ei * 4 + a]]];
+        for (int d = 0; d < ctx->dim; ++d) adj[node * ctx->dim + d] += 1;
+      }
+    }
+    return CFEM_OK;
+  });
+}
+
+cfem_status cfem_bc_mask(const cfem_ctx *ctx, uint8_t *constrained) {
+  return run_guarded([&]() -> cfem_status {
+    check_ctx(ctx);
+    if (!constrained) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "null output"};
+    const Prep &P = ctx->prep;
+    for (int64_t g = 0; g < ctx->nn; ++g) {
+      int64_t o = P.node_new2old[g];
+      for (int d = 0; d < ctx->dim; ++d) constrained[o * ctx->dim + d] = (P.node_bits[g] >> d) & 1u;
+    }
+    return CFEM_OK;
+  });
+}
+
+cfem_status cfem_renumbering(const cfem_ctx *ctx, int32_t *node_new2old, int32_t *elem_new2old) {
+  return run_guarded([&]() -> cfem_status {
+    check_ctx(ctx);
+    if (node_new2old) std::copy(ctx->prep.node_new2old.begin(), ctx->prep.node_new2old.end(), node_new2old);
+    if (elem_new2old) std::copy(ctx->prep.elem_new2old.begin(), ctx->prep.elem_new2old.end(), elem_new2old);
+    return CFEM_OK;
+  });
+}
+
+cfem_status cfem_element_matrices(cfem_ctx *ctx, int64_t first, int64_t count, double *ke) {
+  return run_guarded([&]() -> cfem_status {
+    check_ctx(ctx);
+    if (!ke || first < 0 || count < 0 || first + count > ctx->ne) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "bad element range"};
+    if (count == 0) return CFEM_OK;
+    DBuf<double> out;
+    out.alloc((size_t)count * ctx->w * ctx->w);
+    if (ctx->dim == 3)
+      k_element_matrices<3><<<nblk(count), kThreads, 0, ctx->stream>>>(first, count, ctx->elem_old2new.p, ctx->G64.p, ctx->gstride,
+                                                                        ctx->conn.p, ctx->bits.p, ctx->lam, ctx->mu, out.p);
+    else
+      k_element_matrices<2><<<nblk(count), kThreads, 0, ctx->stream>>>(first, count, ctx->elem_old2new.p, ctx->G64.p, ctx->gstride,
+                                                                        ctx->conn.p, ctx->bits.p, ctx->lam, ctx->mu, out.p);
+    CKL();
+    CK(cudaMemcpyAsync(ke, out.p, sizeof(double) * out.n, cudaMemcpyDefault, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return CFEM_OK;
+  });
+}
+
+cfem_status cfem_diagonal(cfem_ctx *ctx, double *diag) {
+  return run_guarded([&]() -> cfem_status {
+    check_ctx(ctx);
+    if (!diag) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "null output"};
+    to_caller<double>(ctx, ctx->diagK.p, diag);
+    CK(cudaStreamSynchronize(ctx->stream));
+    return CFEM_OK;
+  });
+}
+
+cfem_status cfem_rhs(cfem_ctx *ctx, const cfem_wavelet *w, double t, double *f) {
+  return run_guarded([&]() -> cfem_status {
+    check_ctx(ctx);
+    if (!f) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "null output"};
+    RhsSchedule sch;
+    sch.semantics = ctx->semantics;
+    sch.has_loads = ctx->rhs.has_loads;
+    sch.w = w;
+    double a = 0, b = 0;
+    if (t != 0.0) sch.eval(0.f, a, b);  // initFlocals(0) precedes calcFlocals(t)
+    sch.eval((float)t, a, b);
+    make_rhs(ctx, a, b, ctx->tmp64b.p);
+    to_caller<double>(ctx, ctx->tmp64b.p, f);
+    CK(cudaStreamSynchronize(ctx->stream));
+    return CFEM_OK;
+  });
+}
+
+cfem_status cfem_matvec(cfem_ctx *ctx, int32_t precision, const void *x, void *y) {
+  return run_guarded([&]() -> cfem_status {
+    check_ctx(ctx);
+    if (!x || !y) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "null vector"};
+    if (precision == CFEM_FP64) {
+      to_internal<double>(ctx, (const double *)x, ctx->v64.z.p);
+      MvParams<double> mv = base_mv<double>(ctx);
+      mv.diagA = ctx->diagK.p;
+      mv.x = ctx->v64.z.p;
+      mv.y = ctx->tmp64.p;
+      ctx->tmp64.zero(ctx->stream);
+      launch_mv<double>(ctx, MV_PLAIN, mv);
+      to_caller<double>(ctx, ctx->tmp64.p, (double *)y);
+    } else if (precision == CFEM_FP32) {
+      // float in/out: stage through FP64 conversion buffers
+      DBuf<double> xin;
+      xin.alloc(ctx->nd);
+      DBuf<float> xf;
+      xf.alloc(ctx->nd);
+      CK(cudaMemcpyAsync(xf.p, x, sizeof(float) * ctx->nd, cudaMemcpyDefault, ctx->stream));
+      k_convert<float, double><<<nblk(ctx->nd), kThreads, 0, ctx->stream>>>(ctx->nd, xf.p, xin.p);
+      CKL();
+      to_internal<float>(ctx, xin.p, ctx->v32.z.p);
+      k_convert<double, float><<<nblk(ctx->nvec), kThreads, 0, ctx->stream>>>(ctx->nvec, ctx->diagK.p, ctx->v32.diagA.p);
+      MvParams<float> mv = base_mv<float>(ctx);
+      mv.diagA = ctx->v32.diagA.p;
+      mv.x = ctx->v32.z.p;
+      mv.y = ctx->v32.u.p;
+      ctx->v32.u.zero(ctx->stream);
+      launch_mv<float>(ctx, MV_PLAIN, mv);
+      to_caller<float>(ctx, ctx->v32.u.p, xin.p);
+      k_convert<double, float><<<nblk(ctx->nd), kThreads, 0, ctx->stream>>>(ctx->nd, xin.p, xf.p);
+      CKL();
+      CK(cudaMemcpyAsync(y, xf.p, sizeof(float) * ctx->nd, cudaMemcpyDefault, ctx->stream));
+      ctx->v32.u.zero(ctx->stream);
+    } else {
+      throw Fail{CFEM_ERR_INVALID_ARGUMENT, "matvec precision must be CFEM_FP64 or CFEM_FP32"};
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    return CFEM_OK;
+  });
+}
+
+cfem_status cfem_pcg(cfem_ctx *ctx, const cfem_solve_params *prm, const double *f, double *u, cfem_solve_info *info) {
+  return run_guarded([&]() -> cfem_status {
+    check_ctx(ctx);
+    if (!f || !u) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "null vector"};
+    cfem_solve_params p = prm ? *prm : default_params();
+    to_internal<double>(ctx, f, ctx->v64.f.p);
+    cfem_status st = solve_internal(ctx, &p, info);
+    to_caller<double>(ctx, ctx->v64.x.p, u);
+    CK(cudaStreamSynchronize(ctx->stream));
+    return st;
+  });
+}
+
+cfem_status cfem_static_solve(cfem_ctx *ctx, const cfem_wavelet *w, const cfem_solve_params *prm, double *u,
+                              cfem_solve_info *info) {
+  return run_guarded([&]() -> cfem_status {
+    check_ctx(ctx);
+    if (!u) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "null output"};
+    cfem_solve_params p = prm ? *prm : default_params();
+    RhsSchedule sch;
+    sch.semantics = ctx->semantics;
+    sch.has_loads = ctx->rhs.has_loads;
+    sch.w = w;
+    double a = 0, b = 0;
+    sch.eval(0.f, a, b);  // initFlocals(0, wavelet)
+    make_rhs(ctx, a, b, ctx->v64.f.p);
+    cfem_status st = solve_internal(ctx, &p, info);
+    to_caller<double>(ctx, ctx->v64.x.p, u);
+    CK(cudaStreamSynchronize(ctx->stream));
+    return st;
+  });
+}
+
+}  // extern "C"
+
+// dynamics, multi-RHS and adjoint entry points live in context_dyn.cu

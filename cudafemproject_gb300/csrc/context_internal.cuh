@@ -1,0 +1,198 @@
+// Internals shared by the C-ABI translation units (context.cu, context_dyn.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <functional>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/cfem.h"
+#include "kernels.cuh"
+#include "prep.hpp"
+
+namespace cfem {
+namespace detail {
+
+extern thread_local std::string g_last_error;
+
+struct Fail {
+  cfem_status st;
+  std::string msg;
+};
+
+#define CK(call)                                                                                   \
+  do {                                                                                             \
+    cudaError_t e_ = (call);                                                                       \
+    if (e_ != cudaSuccess)                                                                         \
+      throw Fail{e_ == cudaErrorMemoryAllocation ? CFEM_ERR_OUT_OF_MEMORY : CFEM_ERR_CUDA,          \
+                 std::string(#call) + ": " + cudaGetErrorString(e_)};                              \
+  } while (0)
+
+#define CKL() CK(cudaGetLastError())
+
+template <typename T>
+struct DBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+  ~DBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void alloc(size_t count) {
+    release();
+    if (count == 0) return;
+    CK(cudaMalloc(&p, count * sizeof(T)));
+    n = count;
+  }
+  void zero(cudaStream_t s) {
+    if (p) CK(cudaMemsetAsync(p, 0, n * sizeof(T), s));
+  }
+  void upload(const T *h, size_t count, cudaStream_t s) {
+    alloc(count);
+    if (count) CK(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+  }
+};
+
+template <typename T>
+struct Vecs {
+  DBuf<T> x, r, z, pA, pB, u, f, dinv, diagA;
+};
+
+struct GraphCache {
+  cudaGraphExec_t exec = nullptr;
+  const void *key0 = nullptr;
+  double key1 = 0, key2 = 0;
+  ~GraphCache() { reset(); }
+  void reset() {
+    if (exec) cudaGraphExecDestroy(exec);
+    exec = nullptr;
+  }
+};
+
+inline unsigned nblk(int64_t n, int t = kThreads) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace detail
+}  // namespace cfem
+
+using namespace cfem;
+using namespace cfem::detail;
+
+struct cfem_ctx {
+  cudaStream_t stream = nullptr;
+  int device = 0, n_sm = 0;
+  int dim = 0, nv = 0, w = 0, vw = 0, ncomp = 0;
+  int64_t nn = 0, ne = 0, nd = 0, nvec = 0;
+  int semantics = 0, form = CFEM_FORM_GRADIENT, verbose = 0;
+  double E = 0, nu = 0, rho = 0, lam = 0, mu = 0;
+  Prep prep;
+  RhsParts rhs;
+  std::vector<double> young;  // per-element Young's modulus (caller order), empty if uniform
+  std::vector<int32_t> elems_caller;  // caller connectivity (reference slot order for the re-sorting quirk)
+  double lump_c = 0, cons_c = 0;
+  // mesh on device
+  DBuf<int32_t> elem_off, node_off, nodes, own, node_new2old, elem_new2old, elem_old2new, conn;
+  DBuf<uint2> lconn;
+  DBuf<uint8_t> bits;
+  DBuf<double> coords, escale, young_d;
+  // operator
+  int64_t gstride = 0;
+  DBuf<double> G64, vol, diagK, mlump, mcdiag, mc64;
+  DBuf<float> G32, mc32, diagK32;
+  DBuf<double> FA, FB;
+  DBuf<float> FA32, FB32;
+  // work
+  Vecs<double> v64;
+  Vecs<float> v32;
+  DBuf<double> io, tmp64, tmp64b, rr;
+  DBuf<Scalars> sc;  // [0] FP64 solve, [1] FP32 solve, [2] misc counters
+  DBuf<double> partials;
+  DBuf<unsigned int> counters;
+  DBuf<int> err;
+  Scalars *h_sc = nullptr;
+  double *h_rr = nullptr;
+  int grid_mv = 0, grid_vec = 0;
+  size_t smem64 = 0, smem32 = 0;
+  int chunk = 16;
+  GraphCache graph64, graph32;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // reference re-sorting quirk (compat dynamics)
+  DBuf<int64_t> seg;
+  DBuf<int32_t> perm, node_old2new;
+  DBuf<double> slot_src, slot_tmp;
+
+  ~cfem_ctx() {
+    graph64.reset();
+    graph32.reset();
+    if (h_sc) cudaFreeHost(h_sc);
+    if (h_rr) cudaFreeHost(h_rr);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+  }
+};
+
+
+namespace cfem {
+namespace detail {
+
+struct PcgResult {
+  int status = CFEM_OK;
+  int iters = 0;
+  double gamma0 = 0, gamma = 0, rr = 0, ff = 0;
+};
+
+MvParams<double> base_mv_d(cfem_ctx *c);
+MvParams<float> base_mv_f(cfem_ctx *c);
+void launch_mv_d(cfem_ctx *c, int mode, const MvParams<double> &P);
+void launch_mv_f(cfem_ctx *c, int mode, const MvParams<float> &P);
+PcgResult run_pcg_d(cfem_ctx *c, Vecs<double> &V, double cK, double cM, const double *mcoef, int warm, double tol,
+                    int rule, int maxit);
+PcgResult run_pcg_f(cfem_ctx *c, Vecs<float> &V, float cK, float cM, const float *mcoef, int warm, double tol,
+                    int rule, int maxit);
+void to_internal_d(cfem_ctx *c, const double *src, double *dst, double scale = 1.0);
+void to_internal_f(cfem_ctx *c, const double *src, float *dst, double scale = 1.0);
+void to_caller_d(cfem_ctx *c, const double *src, double *dst);
+void to_caller_f(cfem_ctx *c, const float *src, double *dst);
+void set_diag_vectors(cfem_ctx *c, const double *diagA64);
+void true_residual(cfem_ctx *c, const double *f, const double *x, double *r, float *r32, double &rr, double &ff);
+void make_rhs(cfem_ctx *c, double a, double b, double *dst);
+cfem_status run_guarded(const std::function<cfem_status()> &fn);
+void check_ctx(const cfem_ctx *c);
+cfem_solve_params default_params();
+cfem_status solve_internal(cfem_ctx *c, const cfem_solve_params *prm, cfem_solve_info *info);
+void rebuild_operator(cfem_ctx *c);
+
+template <typename T>
+inline MvParams<T> base_mv(cfem_ctx *c) {
+  if constexpr (sizeof(T) == 8) return base_mv_d(c); else return base_mv_f(c);
+}
+template <typename T>
+inline void launch_mv(cfem_ctx *c, int mode, const MvParams<T> &P) {
+  if constexpr (sizeof(T) == 8) launch_mv_d(c, mode, P); else launch_mv_f(c, mode, P);
+}
+template <typename T>
+inline PcgResult run_pcg(cfem_ctx *c, Vecs<T> &V, T cK, T cM, const T *mcoef, int warm, double tol, int rule, int maxit) {
+  if constexpr (sizeof(T) == 8) return run_pcg_d(c, V, cK, cM, mcoef, warm, tol, rule, maxit);
+  else return run_pcg_f(c, V, cK, cM, mcoef, warm, tol, rule, maxit);
+}
+template <typename T>
+inline void to_internal(cfem_ctx *c, const double *src, T *dst, double scale = 1.0) {
+  if constexpr (sizeof(T) == 8) to_internal_d(c, src, dst, scale); else to_internal_f(c, src, dst, scale);
+}
+template <typename T>
+inline void to_caller(cfem_ctx *c, const T *src, double *dst) {
+  if constexpr (sizeof(T) == 8) to_caller_d(c, src, dst); else to_caller_f(c, src, dst);
+}
+
+}  // namespace detail
+}  // namespace cfem

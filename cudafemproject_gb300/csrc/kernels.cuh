@@ -1,0 +1,434 @@
+// sm_103a kernels of the element-by-element (EbE) elasticity path.
+//
+// Data layout in HBM (all in the locality order built by prep.cpp):
+//  * node vectors: VW values per node (VW = 4 in 3D, 2 in 2D; the pad lane is
+//    kept at zero) so that a node is one 16-byte (FP32) or 32-byte (FP64) load;
+//  * element operator, gradient form: G = sqrt(V * E_e/E) * grad N_a for the
+//    local nodes a = 1..dim (N_0 follows from the partition of unity), stored
+//    structure-of-arrays [ncomp][gstride] so a warp reads 128 coalesced bytes
+//    per component: 36 B per tetrahedron in FP32 (16 B per triangle);
+//  * patches: consecutive runs of elements handled by one CTA, with their node
+//    list (halo nodes first, then the contiguous range the patch owns) and a
+//    16-bit local connectivity (8 B per element).
+//
+// The matvec of a patch (reference: Matrix::bmm u_e = p_e^T K_e then the
+// sort/reduce assembly, femfunc.cpp:66-67 + cpu_fem_utils.cpp:437-459):
+//   stage  : gather the patch's node vectors into shared memory (coalesced,
+//            mostly L2 hits), applying the PCG direction update p = z + beta p
+//            on the fly and masking constrained DOFs;
+//   compute: per element H = sum_a u_a (x) G_a, sigma = lam tr(H) I + mu (H+H^T),
+//            f_a = sigma G_a (+ consistent mass), accumulated with shared atomics;
+//   flush  : one float4 atomicAdd per patch node into the global result.
+// The reference's applyConstraints (cpu_fem_utils.cpp:461-476) keeps K_e's
+// diagonal and zeroes the off-diagonal rows/columns of constrained DOFs, i.e.
+// K' = P K P + (I-P) diag(K); the masked stage/flush realise P K P and the
+// owner of a node adds the (I-P) diag(K) term.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace cfem {
+
+constexpr int kThreads = 256;
+
+struct Scalars {
+  double gamma, gamma_prev, gamma0, sigma;
+  double rr, ff, tol;
+  int rule, maxit, iter, done;  // done: 0 running, 1 converged, 2 diverged, 3 iteration cap
+  unsigned int count_mv, count_up;
+  int pad0, pad1;
+};
+
+struct DynState {
+  int step;
+  unsigned int count;
+  int pad0, pad1;
+};
+
+// ------------------------------------------------------------------ helpers
+template <typename T, int VW>
+struct NodeV {
+  T v[VW];
+};
+
+template <typename T, int VW>
+__device__ __forceinline__ NodeV<T, VW> ldv(const T *p, int64_t node) {
+  NodeV<T, VW> r;
+  if constexpr (sizeof(T) == 4 && VW == 4) {
+    float4 a = reinterpret_cast<const float4 *>(p)[node];
+    r.v[0] = a.x; r.v[1] = a.y; r.v[2] = a.z; r.v[3] = a.w;
+  } else if constexpr (sizeof(T) == 4 && VW == 2) {
+    float2 a = reinterpret_cast<const float2 *>(p)[node];
+    r.v[0] = a.x; r.v[1] = a.y;
+  } else if constexpr (VW == 4) {
+    double2 a = reinterpret_cast<const double2 *>(p)[2 * node];
+    double2 b = reinterpret_cast<const double2 *>(p)[2 * node + 1];
+    r.v[0] = a.x; r.v[1] = a.y; r.v[2] = b.x; r.v[3] = b.y;
+  } else {
+    double2 a = reinterpret_cast<const double2 *>(p)[node];
+    r.v[0] = a.x; r.v[1] = a.y;
+  }
+  return r;
+}
+
+template <typename T, int VW>
+__device__ __forceinline__ void stv(T *p, int64_t node, const NodeV<T, VW> &r) {
+  if constexpr (sizeof(T) == 4 && VW == 4) {
+    reinterpret_cast<float4 *>(p)[node] = make_float4(r.v[0], r.v[1], r.v[2], r.v[3]);
+  } else if constexpr (sizeof(T) == 4 && VW == 2) {
+    reinterpret_cast<float2 *>(p)[node] = make_float2(r.v[0], r.v[1]);
+  } else if constexpr (VW == 4) {
+    reinterpret_cast<double2 *>(p)[2 * node] = make_double2(r.v[0], r.v[1]);
+    reinterpret_cast<double2 *>(p)[2 * node + 1] = make_double2(r.v[2], r.v[3]);
+  } else {
+    reinterpret_cast<double2 *>(p)[node] = make_double2(r.v[0], r.v[1]);
+  }
+}
+
+template <typename T, int VW>
+__device__ __forceinline__ void atomic_addv(T *p, int64_t node, const NodeV<T, VW> &r, int dim) {
+  if constexpr (sizeof(T) == 4 && VW == 4) {
+    atomicAdd(reinterpret_cast<float4 *>(p) + node, make_float4(r.v[0], r.v[1], r.v[2], 0.f));
+  } else if constexpr (sizeof(T) == 4 && VW == 2) {
+    atomicAdd(reinterpret_cast<float2 *>(p) + node, make_float2(r.v[0], r.v[1]));
+  } else {
+    for (int d = 0; d < dim; ++d) atomicAdd(p + node * VW + d, r.v[d]);
+  }
+}
+
+// Sum N doubles over the block; result valid in thread 0.
+template <int N>
+__device__ __forceinline__ void block_sum(double (&v)[N]) {
+  __shared__ double red[N][kThreads / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    double x = v[k];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) red[k][wid] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      double s = 0;
+      for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += red[k][i];
+      v[k] = s;
+    }
+  }
+  __syncthreads();
+}
+
+// Publishes this block's partial sums; returns true in thread 0 of the last
+// block to finish, which then holds the grid totals (summed in block order, so
+// the result does not depend on scheduling).
+template <int N>
+__device__ __forceinline__ bool grid_sum_last(double (&v)[N], double *partials, unsigned int *count) {
+  block_sum<N>(v);
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) partials[(size_t)blockIdx.x * N + k] = v[k];
+    __threadfence();
+    unsigned int t = atomicAdd(count, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  // every block's partials are visible; sum them in block order
+  double s[N];
+#pragma unroll
+  for (int k = 0; k < N; ++k) s[k] = 0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+#pragma unroll
+    for (int k = 0; k < N; ++k) s[k] += __ldcg(partials + (size_t)b * N + k);
+  // fixed-order block reduction of the strided sums
+  __shared__ double red2[N][kThreads];
+#pragma unroll
+  for (int k = 0; k < N; ++k) red2[k][threadIdx.x] = s[k];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < N; ++k) {
+      double t = 0;
+      for (int i = 0; i < (int)blockDim.x; ++i) t += red2[k][i];
+      v[k] = t;
+    }
+    *count = 0;
+  }
+  return threadIdx.x == 0;
+}
+
+// ------------------------------------------------------------------ element kernel
+// Stiffness (and consistent mass) action of one element in gradient form.
+// u[a][d]: masked nodal values; G: dim*dim gradient components of nodes 1..dim.
+template <typename T, int DIM>
+__device__ __forceinline__ void element_force(const T (&u)[DIM + 1][DIM], const T (&G)[DIM * DIM], T lam, T mu,
+                                              T cK, T mcoef, T (&f)[DIM + 1][DIM]) {
+  T H[DIM][DIM];
+#pragma unroll
+  for (int i = 0; i < DIM; ++i)
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) {
+      T h = 0;
+#pragma unroll
+      for (int a = 1; a <= DIM; ++a) h += (u[a][i] - u[0][i]) * G[(a - 1) * DIM + j];
+      H[i][j] = h;
+    }
+  T tr = 0;
+#pragma unroll
+  for (int i = 0; i < DIM; ++i) tr += H[i][i];
+  T S[DIM][DIM];
+#pragma unroll
+  for (int i = 0; i < DIM; ++i)
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) S[i][j] = cK * (mu * (H[i][j] + H[j][i]) + (i == j ? lam * tr : T(0)));
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) f[0][d] = 0;
+#pragma unroll
+  for (int a = 1; a <= DIM; ++a)
+#pragma unroll
+    for (int i = 0; i < DIM; ++i) {
+      T s = 0;
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) s += S[i][j] * G[(a - 1) * DIM + j];
+      f[a][i] = s;
+      f[0][i] -= s;
+    }
+  if (mcoef != T(0)) {
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      T sum = 0;
+#pragma unroll
+      for (int a = 0; a <= DIM; ++a) sum += u[a][d];
+#pragma unroll
+      for (int a = 0; a <= DIM; ++a) f[a][d] += mcoef * (u[a][d] + sum);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ matvec
+enum MvMode { MV_PLAIN = 0, MV_PCG = 1, MV_DYN = 2 };
+
+template <typename T>
+struct MvParams {
+  int n_patches;
+  const int32_t *elem_off, *node_off, *nodes, *own;
+  const uint2 *lconn;
+  const uint8_t *bits;
+  const T *G;        // [ncomp][gstride]
+  int64_t gstride;
+  const T *mcoef;    // per element consistent-mass coefficient, or nullptr
+  T lam, mu, cK, cM;
+  const T *diagA;    // node vectors: diagonal of the operator (used on constrained DOFs)
+  const T *x;        // PLAIN: x; PCG: z; DYN: d_old
+  const T *x2;       // PCG: p_old; DYN: v
+  const T *x3;       // DYN: a
+  T *xout;           // PCG: p_new; DYN: d_new (owned nodes only)
+  T *y;              // result accumulation (zero on entry)
+  Scalars *sc;       // PCG scalars (beta in, sigma out)
+  double *partials;  // [gridDim] partial sums of p.Ap
+  T c1, c2;          // DYN: d_new = d + c1 v + c2 a
+};
+
+template <typename T, int DIM, int MODE>
+__global__ void __launch_bounds__(kThreads) k_matvec(MvParams<T> P) {
+  constexpr int VW = DIM == 3 ? 4 : 2;
+  constexpr int NC = DIM * DIM;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *sp = reinterpret_cast<T *>(smem_raw);
+  if (MODE == MV_PCG && P.sc->done) return;
+  T beta = 0;
+  if (MODE == MV_PCG) beta = P.sc->iter == 0 ? T(0) : T(P.sc->gamma / P.sc->gamma_prev);
+  const int np_cap = 0;  // unused
+  (void)np_cap;
+  double energy = 0;
+  for (int patch = blockIdx.x; patch < P.n_patches; patch += gridDim.x) {
+    const int nb = P.node_off[patch], nn = P.node_off[patch + 1] - nb, own = P.own[patch];
+    const int e0 = P.elem_off[patch], ne = P.elem_off[patch + 1] - e0;
+    T *sy = sp + (size_t)nn * VW;
+    // stage
+    for (int i = threadIdx.x; i < nn; i += blockDim.x) {
+      const int g = P.nodes[nb + i];
+      NodeV<T, VW> v = ldv<T, VW>(P.x, g);
+      if (MODE == MV_PCG) {
+        if (beta != T(0)) {
+          NodeV<T, VW> po = ldv<T, VW>(P.x2, g);
+#pragma unroll
+          for (int d = 0; d < DIM; ++d) v.v[d] += beta * po.v[d];
+        }
+        if (i >= own) stv<T, VW>(P.xout, g, v);
+      } else if (MODE == MV_DYN) {
+        NodeV<T, VW> vv = ldv<T, VW>(P.x2, g), aa = ldv<T, VW>(P.x3, g);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) v.v[d] += P.c1 * vv.v[d] + P.c2 * aa.v[d];
+        if (i >= own) stv<T, VW>(P.xout, g, v);
+      }
+      const unsigned b = P.bits[g];
+#pragma unroll
+      for (int d = 0; d < VW; ++d) {
+        sp[(size_t)i * VW + d] = (d < DIM && !(b >> d & 1u)) ? v.v[d] : T(0);
+        sy[(size_t)i * VW + d] = 0;
+      }
+    }
+    __syncthreads();
+    // compute
+    for (int le = threadIdx.x; le < ne; le += blockDim.x) {
+      const int e = e0 + le;
+      const uint2 c = P.lconn[e];
+      int li[4] = {(int)(c.x & 0xffffu), (int)(c.x >> 16), (int)(c.y & 0xffffu), (int)(c.y >> 16)};
+      T G[NC];
+#pragma unroll
+      for (int k = 0; k < NC; ++k) G[k] = P.G[(size_t)k * P.gstride + e];
+      T u[DIM + 1][DIM], f[DIM + 1][DIM];
+#pragma unroll
+      for (int a = 0; a <= DIM; ++a)
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) u[a][d] = sp[(size_t)li[a] * VW + d];
+      const T mc = P.mcoef ? P.cM * P.mcoef[e] : T(0);
+      element_force<T, DIM>(u, G, P.lam, P.mu, P.cK, mc, f);
+#pragma unroll
+      for (int a = 0; a <= DIM; ++a)
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+          if (MODE == MV_PCG) energy += (double)(u[a][d] * f[a][d]);
+          atomicAdd(sy + (size_t)li[a] * VW + d, f[a][d]);
+        }
+    }
+    __syncthreads();
+    // flush
+    for (int i = threadIdx.x; i < nn; i += blockDim.x) {
+      const int g = P.nodes[nb + i];
+      const unsigned b = P.bits[g];
+      NodeV<T, VW> r;
+      bool any = false;
+#pragma unroll
+      for (int d = 0; d < VW; ++d) {
+        T val = (d < DIM && !(b >> d & 1u)) ? sy[(size_t)i * VW + d] : T(0);
+        r.v[d] = val;
+        any |= val != T(0);
+      }
+      if (b && i >= own) {
+        // (I - P) diag(A) x on the constrained DOFs of an owned node
+        NodeV<T, VW> v = ldv<T, VW>(P.x, g);
+        if (MODE == MV_PCG && beta != T(0)) {
+          NodeV<T, VW> po = ldv<T, VW>(P.x2, g);
+#pragma unroll
+          for (int d = 0; d < DIM; ++d) v.v[d] += beta * po.v[d];
+        } else if (MODE == MV_DYN) {
+          NodeV<T, VW> vv = ldv<T, VW>(P.x2, g), aa = ldv<T, VW>(P.x3, g);
+#pragma unroll
+          for (int d = 0; d < DIM; ++d) v.v[d] += P.c1 * vv.v[d] + P.c2 * aa.v[d];
+        }
+        NodeV<T, VW> dg = ldv<T, VW>(P.diagA, g);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d)
+          if (b >> d & 1u) {
+            T t = dg.v[d] * v.v[d];
+            r.v[d] = t;
+            any |= t != T(0);
+            if (MODE == MV_PCG) energy += (double)(t * v.v[d]);
+          }
+      }
+      if (any) atomic_addv<T, VW>(P.y, g, r, DIM);
+    }
+    __syncthreads();
+  }
+  if (MODE == MV_PCG) {
+    double v[1] = {energy};
+    if (grid_sum_last<1>(v, P.partials, &P.sc->count_mv)) P.sc->sigma = v[0];
+  }
+}
+
+// ------------------------------------------------------------------ PCG vector kernels
+template <typename T>
+struct VecParams {
+  int64_t n_nodes;
+  T *x, *r, *z, *p, *u;
+  const T *dinv;
+  const T *f;        // init: right-hand side
+  Scalars *sc;
+  double *partials;
+};
+
+// r = f - u (warm) or f; x = 0 unless warm; z = M^-1 r; u = 0; gamma0 = r.z
+template <typename T, int DIM>
+__global__ void __launch_bounds__(kThreads) k_pcg_init(VecParams<T> P, int warm) {
+  constexpr int VW = DIM == 3 ? 4 : 2;
+  double acc[3] = {0, 0, 0};  // r.z, r.r, f.f
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < P.n_nodes; n += (int64_t)gridDim.x * blockDim.x) {
+    NodeV<T, VW> f = ldv<T, VW>(P.f, n), di = ldv<T, VW>(P.dinv, n), r, z, zero;
+    NodeV<T, VW> u = ldv<T, VW>(P.u, n);
+#pragma unroll
+    for (int d = 0; d < VW; ++d) { zero.v[d] = 0; r.v[d] = 0; z.v[d] = 0; }
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      r.v[d] = warm ? f.v[d] - u.v[d] : f.v[d];
+      z.v[d] = r.v[d] * di.v[d];
+      acc[0] += (double)r.v[d] * (double)z.v[d];
+      acc[1] += (double)r.v[d] * (double)r.v[d];
+      acc[2] += (double)f.v[d] * (double)f.v[d];
+    }
+    stv<T, VW>(P.r, n, r);
+    stv<T, VW>(P.z, n, z);
+    stv<T, VW>(P.u, n, zero);
+    if (!warm) stv<T, VW>(P.x, n, zero);
+  }
+  if (grid_sum_last<3>(acc, P.partials, &P.sc->count_up)) {
+    Scalars *s = P.sc;
+    s->gamma0 = s->gamma = s->gamma_prev = acc[0];
+    s->rr = acc[1];
+    s->ff = acc[2];
+    s->iter = 0;
+    s->sigma = 0;
+    int done = 0;
+    if (acc[0] == 0.0) done = 1;
+    if (s->rule == 1 && sqrt(acc[1]) <= s->tol * sqrt(acc[2])) done = 1;
+    if (!isfinite(acc[0])) done = 2;
+    s->done = done;
+  }
+}
+
+// alpha = gamma / p.Ap; x += alpha p; r -= alpha u; u = 0; z = M^-1 r; gamma' = r.z
+template <typename T, int DIM>
+__global__ void __launch_bounds__(kThreads) k_pcg_update(VecParams<T> P) {
+  constexpr int VW = DIM == 3 ? 4 : 2;
+  Scalars *s = P.sc;
+  if (s->done) return;
+  const double alpha_d = s->gamma / s->sigma;
+  const T alpha = (T)alpha_d;
+  double acc[2] = {0, 0};
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < P.n_nodes; n += (int64_t)gridDim.x * blockDim.x) {
+    NodeV<T, VW> x = ldv<T, VW>(P.x, n), r = ldv<T, VW>(P.r, n), p = ldv<T, VW>(P.p, n), u = ldv<T, VW>(P.u, n);
+    NodeV<T, VW> di = ldv<T, VW>(P.dinv, n), z, zero;
+#pragma unroll
+    for (int d = 0; d < VW; ++d) { zero.v[d] = 0; z.v[d] = 0; }
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      x.v[d] += alpha * p.v[d];
+      r.v[d] -= alpha * u.v[d];
+      z.v[d] = r.v[d] * di.v[d];
+      acc[0] += (double)r.v[d] * (double)z.v[d];
+      acc[1] += (double)r.v[d] * (double)r.v[d];
+    }
+    stv<T, VW>(P.x, n, x);
+    stv<T, VW>(P.r, n, r);
+    stv<T, VW>(P.z, n, z);
+    stv<T, VW>(P.u, n, zero);
+  }
+  if (grid_sum_last<2>(acc, P.partials, &s->count_up)) {
+    s->gamma_prev = s->gamma;
+    s->gamma = acc[0];
+    s->rr = acc[1];
+    s->iter += 1;
+    int done = 0;
+    if (!isfinite(acc[0]) || !isfinite(alpha_d)) done = 2;
+    else if (s->rule == 0 && acc[0] < s->tol * s->gamma0) done = 1;
+    else if (s->rule == 1 && sqrt(acc[1]) <= s->tol * sqrt(s->ff)) done = 1;
+    else if (s->iter >= s->maxit) done = 3;
+    s->done = done;
+  }
+}
+
+}  // namespace cfem

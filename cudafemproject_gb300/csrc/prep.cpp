@@ -1,0 +1,308 @@
+// Host-side mesh preparation; see prep.hpp.
+#include "prep.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+namespace cfem {
+
+namespace {
+
+inline uint64_t spread3(uint64_t v) {  // 21 bits -> every third bit
+  v &= 0x1fffff;
+  v = (v | v << 32) & 0x1f00000000ffffULL;
+  v = (v | v << 16) & 0x1f0000ff0000ffULL;
+  v = (v | v << 8) & 0x100f00f00f00f00fULL;
+  v = (v | v << 4) & 0x10c30c30c30c30c3ULL;
+  v = (v | v << 2) & 0x1249249249249249ULL;
+  return v;
+}
+
+inline uint64_t spread2(uint64_t v) {  // 32 bits -> every second bit
+  v &= 0xffffffffULL;
+  v = (v | v << 16) & 0x0000ffff0000ffffULL;
+  v = (v | v << 8) & 0x00ff00ff00ff00ffULL;
+  v = (v | v << 4) & 0x0f0f0f0f0f0f0f0fULL;
+  v = (v | v << 2) & 0x3333333333333333ULL;
+  v = (v | v << 1) & 0x5555555555555555ULL;
+  return v;
+}
+
+}  // namespace
+
+std::string build_prep(const cfem_mesh &m, int patch_elems, Prep &P) {
+  const int dim = m.dim;
+  if (dim != 2 && dim != 3) return "dim must be 2 or 3";
+  if (m.n_nodes <= 0 || m.n_elems <= 0) return "mesh has no nodes or no elements";
+  if (m.n_nodes > (int64_t)INT32_MAX / 4 || m.n_elems > (int64_t)INT32_MAX / 12) return "mesh too large for int32 DOF ids";
+  const int nv = dim + 1;
+  P.dim = dim; P.nv = nv; P.w = 6 * (dim - 1);
+  P.nn = m.n_nodes; P.ne = m.n_elems;
+  P.patch_elems = patch_elems;
+  const int64_t nn = m.n_nodes, ne = m.n_elems;
+  std::vector<int32_t> used(nn, 0);
+  for (int64_t i = 0; i < ne * nv; ++i) {
+    int32_t v = m.elems[i];
+    if (v < 0 || v >= nn) return "element " + std::to_string(i / nv) + " references node " + std::to_string(v) + " out of range";
+    used[v] = 1;
+  }
+  for (int64_t i = 0; i < nn; ++i)
+    if (!used[i])
+      return "node " + std::to_string(i) + " belongs to no element (the reference compacts DOF ids, so every node must be used)";
+  for (int64_t e = 0; e < ne; ++e)
+    for (int a = 0; a < nv; ++a)
+      for (int b = a + 1; b < nv; ++b)
+        if (m.elems[e * nv + a] == m.elems[e * nv + b]) return "element " + std::to_string(e) + " repeats a node";
+
+  // ---- Morton order of element centroids (isotropic quantisation) ----
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  for (int64_t i = 0; i < nn; ++i)
+    for (int d = 0; d < dim; ++d) {
+      double x = m.nodes[i * dim + d];
+      if (!std::isfinite(x)) return "node " + std::to_string(i) + " has a non-finite coordinate";
+      lo[d] = std::min(lo[d], x); hi[d] = std::max(hi[d], x);
+    }
+  double ext = 0;
+  for (int d = 0; d < dim; ++d) ext = std::max(ext, hi[d] - lo[d]);
+  if (ext <= 0) ext = 1;
+  const double qmax = dim == 3 ? 2097151.0 : 4294967295.0;
+  std::vector<std::pair<uint64_t, int32_t>> key(ne);
+  for (int64_t e = 0; e < ne; ++e) {
+    double c[3] = {0, 0, 0};
+    for (int a = 0; a < nv; ++a)
+      for (int d = 0; d < dim; ++d) c[d] += m.nodes[(int64_t)m.elems[e * nv + a] * dim + d];
+    uint64_t q[3] = {0, 0, 0};
+    for (int d = 0; d < dim; ++d) {
+      double t = (c[d] / nv - lo[d]) / ext;
+      t = std::min(std::max(t, 0.0), 1.0);
+      q[d] = (uint64_t)(t * qmax);
+    }
+    uint64_t k = dim == 3 ? (spread3(q[0]) | spread3(q[1]) << 1 | spread3(q[2]) << 2) : (spread2(q[0]) | spread2(q[1]) << 1);
+    key[e] = {k, (int32_t)e};
+  }
+  std::sort(key.begin(), key.end());
+  P.elem_new2old.resize(ne);
+  P.elem_old2new.resize(ne);
+  for (int64_t i = 0; i < ne; ++i) {
+    P.elem_new2old[i] = key[i].second;
+    P.elem_old2new[key[i].second] = (int32_t)i;
+  }
+  key.clear();
+  key.shrink_to_fit();
+
+  // ---- patches and first-touch node numbering ----
+  const int pe = patch_elems;
+  P.n_patches = (int)((ne + pe - 1) / pe);
+  P.node_old2new.assign(nn, -1);
+  P.node_new2old.resize(nn);
+  int32_t next = 0;
+  std::vector<int32_t> first_new(P.n_patches + 1, 0);
+  for (int p = 0; p < P.n_patches; ++p) {
+    first_new[p] = next;
+    int64_t e1 = std::min<int64_t>(ne, (int64_t)(p + 1) * pe);
+    for (int64_t ei = (int64_t)p * pe; ei < e1; ++ei) {
+      int64_t e = P.elem_new2old[ei];
+      for (int a = 0; a < nv; ++a) {
+        int32_t o = m.elems[e * nv + a];
+        if (P.node_old2new[o] < 0) {
+          P.node_old2new[o] = next;
+          P.node_new2old[next] = o;
+          ++next;
+        }
+      }
+    }
+  }
+  first_new[P.n_patches] = next;
+  P.p_elem_off.resize(P.n_patches + 1);
+  P.p_node_off.resize(P.n_patches + 1);
+  P.p_own.resize(P.n_patches);
+  P.p_nodes.clear();
+  P.p_nodes.reserve((size_t)(nn * 1.6) + 16);
+  P.lconn.assign(ne * 4, 0);
+  std::vector<int32_t> mark(nn, -1), loc(nn, 0);
+  std::vector<int32_t> list;
+  P.np_max = 0;
+  for (int p = 0; p < P.n_patches; ++p) {
+    int64_t e0 = (int64_t)p * pe, e1 = std::min<int64_t>(ne, e0 + pe);
+    P.p_elem_off[p] = (int32_t)e0;
+    list.clear();
+    for (int64_t ei = e0; ei < e1; ++ei) {
+      int64_t e = P.elem_new2old[ei];
+      for (int a = 0; a < nv; ++a) {
+        int32_t g = P.node_old2new[m.elems[e * nv + a]];
+        if (mark[g] != p) { mark[g] = p; list.push_back(g); }
+      }
+    }
+    std::sort(list.begin(), list.end());
+    if (list.size() > 65535) return "patch has more than 65535 nodes";
+    P.p_node_off[p] = (int32_t)P.p_nodes.size();
+    int own = (int)(std::lower_bound(list.begin(), list.end(), first_new[p]) - list.begin());
+    P.p_own[p] = own;
+    for (size_t i = 0; i < list.size(); ++i) { loc[list[i]] = (int32_t)i; P.p_nodes.push_back(list[i]); }
+    P.np_max = std::max<int>(P.np_max, (int)list.size());
+    for (int64_t ei = e0; ei < e1; ++ei) {
+      int64_t e = P.elem_new2old[ei];
+      for (int a = 0; a < nv; ++a) P.lconn[ei * 4 + a] = (uint16_t)loc[P.node_old2new[m.elems[e * nv + a]]];
+    }
+  }
+  P.p_elem_off[P.n_patches] = (int32_t)ne;
+  P.p_node_off[P.n_patches] = (int32_t)P.p_nodes.size();
+
+  // ---- constraints (datakeeper.cpp:139-171) ----
+  P.dof_bc.assign(nn * dim, 0);
+  P.ctype.assign(nn, 0);
+  for (int64_t i = 0; i < m.n_constraints; ++i) {
+    int32_t node = m.constraints[2 * i], type = m.constraints[2 * i + 1];
+    if (node < 0 || node >= nn) return "constraint " + std::to_string(i) + " names node " + std::to_string(node) + " out of range";
+    P.ctype[node] = type;
+    if (type & 1) P.dof_bc[(int64_t)dim * node + 0] = 1;
+    if (type & 2) P.dof_bc[(int64_t)dim * node + 1] = 1;
+    if (dim == 3 && (type & 3)) P.dof_bc[(int64_t)dim * node + 2] = 1;
+  }
+  P.node_bits.assign(nn, 0);
+  for (int64_t o = 0; o < nn; ++o) {
+    uint8_t b = 0;
+    for (int d = 0; d < dim; ++d)
+      if (P.dof_bc[o * dim + d]) b |= (uint8_t)(1u << d);
+    P.node_bits[P.node_old2new[o]] = b;
+  }
+  return "";
+}
+
+float wavelet_value(const cfem_wavelet *w, float t) {
+  if (!w) return 0.f;
+  const float ts = (float)w->timeshift;
+  if (t < ts) return 0.f;
+  const float ampl = (float)w->ampl, freq = (float)w->freq;
+  t = t - ts;
+  if (w->type == CFEM_WAVELET_RICKER) {
+    float tmp = (float)(M_PI * freq * t - M_PI);
+    return ampl * (1.f - 2.f * tmp * tmp) * std::exp(-1.f * tmp * tmp);
+  }
+  if (w->type == CFEM_WAVELET_BERLAGE) {
+    float w0 = (float)(2 * M_PI * freq);
+    float w1 = w0 / std::sqrt(3.f);
+    return ampl * w1 * w1 / 4.f * std::exp(-1.f * w1 * t) *
+           (std::sin(w0 * t) * (1.f / (w1 * w1 * w1) + t / (w1 * w1) - t * t / w1) -
+            std::cos(w0 * t) * std::sqrt(3.f) * (t * t / w1 + t / (w1 * w1)));
+  }
+  return 0.f;
+}
+
+void RhsSchedule::eval(float t, double &a, double &b) {
+  if (semantics == CFEM_CONSISTENT) {
+    if (!w || w->type == CFEM_WAVELET_NONE) { a = 1; b = 0; return; }
+    a = w->ampl != 0 ? (double)wavelet_value(w, t) / w->ampl : 0.0;
+    b = 0;
+    return;
+  }
+  float v = wavelet_value(w, t);
+  if (v != 0.f) { state_is_wavelet = true; state_value = v; }
+  if (has_loads) { a = 0; b = 1; return; }  // calcLoads overwrites every slot
+  if (state_is_wavelet) { a = state_value; b = 0; } else { a = 0; b = 1; }
+}
+
+std::string build_rhs(const cfem_mesh &m, const Prep &P, int semantics, RhsParts &out) {
+  const int dim = m.dim, nv = dim + 1, w = 6 * (dim - 1);
+  const int64_t nd = m.n_nodes * dim;
+  out.FA.assign(nd, 0.0);
+  out.FB.assign(nd, 0.0);
+  out.has_loads = m.n_loads > 0;
+  // normalised face normals and face measures (datakeeper.cpp:201-209, cpu_fem_utils.cpp:247-272)
+  std::vector<double> nrm(m.n_faces * dim), flen(m.n_faces), fmeas(m.n_faces);
+  for (int64_t f = 0; f < m.n_faces; ++f) {
+    double l2 = 0;
+    for (int j = 0; j < dim; ++j) l2 += m.face_normals[f * dim + j] * m.face_normals[f * dim + j];
+    if (!(l2 > 0)) return "face " + std::to_string(f) + " has a zero normal";
+    for (int j = 0; j < dim; ++j) nrm[f * dim + j] = m.face_normals[f * dim + j] / std::sqrt(l2);
+    for (int i = 0; i < nv; ++i) {
+      int32_t v = m.face_nodes[f * nv + i];
+      if (v < 0 || v >= m.n_nodes) return "face " + std::to_string(f) + " names node out of range";
+    }
+    if (m.face_elems[f] < 0 || m.face_elems[f] >= m.n_elems) return "face " + std::to_string(f) + " names element out of range";
+    const double *a = m.nodes + (int64_t)m.face_nodes[f * nv + 0] * dim;
+    const double *b = m.nodes + (int64_t)m.face_nodes[f * nv + 1] * dim;
+    if (dim == 2) {
+      double L = std::sqrt((b[0] - a[0]) * (b[0] - a[0]) + (b[1] - a[1]) * (b[1] - a[1]));
+      flen[f] = L;          // reference measure
+      fmeas[f] = 0.5 * L;   // consistent: t*L/2 per node
+    } else {
+      const double *c = m.nodes + (int64_t)m.face_nodes[f * nv + 2] * dim;
+      double ax = b[0] - a[0], ay = b[1] - a[1], az = b[2] - a[2];
+      double bx = c[0] - a[0], by = c[1] - a[1], bz = c[2] - a[2];
+      double c1 = ay * bz - az * by, c2 = az * bx - ax * bz, c3 = ax * by - ay * bx;
+      double cr2 = c1 * c1 + c2 * c2 + c3 * c3;
+      flen[f] = 0.5 * cr2;                   // reference: 0.5*|a x b|^2 (no square root)
+      fmeas[f] = 0.5 * std::sqrt(cr2) / 3.0;  // consistent: t*A/3 per node
+    }
+  }
+  if (semantics == CFEM_COMPAT) {
+    if (out.has_loads) {
+      // calcLoads: nodal load array (last entry wins) gathered into every element
+      // slot, then assembled: each DOF gets load * (number of adjacent elements).
+      std::vector<double> loads(nd, 0.0);
+      std::vector<int32_t> adj(m.n_nodes, 0);
+      for (int64_t i = 0; i < m.n_elems * nv; ++i) adj[m.elems[i]]++;
+      for (int64_t l = 0; l < m.n_loads; ++l) {
+        int32_t node = m.load_nodes[l];
+        if (node < 0 || node >= m.n_nodes) return "load " + std::to_string(l) + " names node out of range";
+        for (int d = 0; d < dim; ++d) loads[(int64_t)dim * node + d] = m.load_vectors[l * dim + d];
+      }
+      for (int64_t k = 0; k < nd; ++k) out.FB[k] = loads[k] * adj[k / dim];
+      return "";
+    }
+    // calcPressures: each face writes (not adds) coeff*p*L*n_j into the element
+    // slot of its nodes; the last face to write a slot wins. Q5: component j is
+    // zeroed when (constraint code of the node) & j.
+    const double coeff = dim == 2 ? -0.5 : -1.0 / 12.0;
+    std::vector<double> slotA((size_t)m.n_elems * w, 0.0), slotB((size_t)m.n_elems * w, 0.0);
+    std::vector<uint8_t> touched((size_t)m.n_elems * w, 0);
+    for (int64_t f = 0; f < m.n_faces; ++f) {
+      int64_t e = m.face_elems[f];
+      for (int i = 0; i < dim; ++i) {
+        int32_t node = m.face_nodes[f * nv + i];
+        int loc = -1;
+        for (int a = 0; a < nv; ++a)
+          if (m.elems[e * nv + a] == node) { loc = a; break; }
+        if (loc < 0) continue;  // reference prints "Wrong index" and writes out of range; skipped here
+        for (int j = 0; j < dim; ++j) {
+          bool masked = (P.ctype[node] & j) != 0;
+          size_t s = (size_t)e * w + dim * loc + j;
+          slotA[s] = masked ? 0.0 : coeff * 1.0 * flen[f] * nrm[f * dim + j];
+          slotB[s] = masked ? 0.0 : coeff * m.face_pressures[f] * flen[f] * nrm[f * dim + j];
+          touched[s] = 1;
+        }
+      }
+    }
+    for (int64_t e = 0; e < m.n_elems; ++e)
+      for (int a = 0; a < nv; ++a)
+        for (int j = 0; j < dim; ++j) {
+          size_t s = (size_t)e * w + dim * a + j;
+          if (!touched[s]) continue;
+          int64_t dof = (int64_t)dim * m.elems[e * nv + a] + j;
+          out.FA[dof] += slotA[s];
+          out.FB[dof] += slotB[s];
+        }
+    return "";
+  }
+  // consistent: accumulate t*L/2 (2D) or t*A/3 (3D) per face node plus point
+  // loads once; constrained DOFs get no load.
+  for (int64_t f = 0; f < m.n_faces; ++f)
+    for (int i = 0; i < dim; ++i) {
+      int32_t node = m.face_nodes[f * nv + i];
+      for (int j = 0; j < dim; ++j)
+        out.FA[(int64_t)dim * node + j] += -m.face_pressures[f] * fmeas[f] * nrm[f * dim + j];
+    }
+  for (int64_t l = 0; l < m.n_loads; ++l) {
+    int32_t node = m.load_nodes[l];
+    if (node < 0 || node >= m.n_nodes) return "load " + std::to_string(l) + " names node out of range";
+    for (int d = 0; d < dim; ++d) out.FA[(int64_t)dim * node + d] += m.load_vectors[l * dim + d];
+  }
+  for (int64_t k = 0; k < nd; ++k)
+    if (P.dof_bc[k]) out.FA[k] = 0;
+  return "";
+}
+
+}  // namespace cfem

@@ -1,0 +1,220 @@
+/*
+ * cfem.h -- C-ABI of the GB300 (sm_103a) element-by-element elasticity library.
+ *
+ * The reference (moarseniy/CudaFEMproject) exposes its path as C++ free
+ * functions over a DEVICE_NAME switch (FEMproject/femfunc/src/femfunc.h:20-24)
+ * plus the ElementsData / Matrix factories
+ * (FEMproject/fem_utils/include/fem_utils_cpu.h:24-148,
+ *  FEMproject/matrix_pack/include/matrix_pack_cpu.h:31-121). This header is the
+ * flat boundary those calls map onto: plain pointers and sizes, status codes,
+ * no C++ or torch types. The C++ mirror of the reference interface
+ * (include/cfem_femfunc.hpp) and the Python driver both sit on top of it.
+ *
+ * Conventions
+ *  - Every call returns a cfem_status; nothing exits the process (the reference
+ *    calls exit() on assertion and NaN, Tools.cpp:27-33 / femfunc.cpp:107-110).
+ *    cfem_last_error_string() gives the message of the last failure.
+ *  - Vectors (displacements, right-hand sides) are in the caller's node order,
+ *    DIM values per node, like dataKeeper::get_displacements()
+ *    (datakeeper.cpp:64-66). Unless stated otherwise an array argument may be
+ *    host memory or device memory of the context's GPU (copied with
+ *    cudaMemcpyDefault on the context's stream).
+ *  - One context per stream; no global mutable state besides the per-thread
+ *    error string (replaces the reference's static cuBLAS handle,
+ *    cuda_matrix.cpp:3-8).
+ */
+#ifndef CFEM_H
+#define CFEM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CFEM_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define CFEM_API __attribute__((visibility("default")))
+#else
+#define CFEM_API
+#endif
+
+typedef enum cfem_status {
+  CFEM_OK = 0,
+  CFEM_ERR_INVALID_ARGUMENT = 1,
+  CFEM_ERR_CUDA = 2,
+  CFEM_ERR_OUT_OF_MEMORY = 3,
+  CFEM_ERR_NOT_CONVERGED = 4,  /* iteration cap reached before the stopping rule */
+  CFEM_ERR_DIVERGED = 5,       /* NaN / Inf in the PCG scalars (reference: exit(-1)) */
+  CFEM_ERR_MESH = 6,           /* inconsistent mesh (bad ids, unused nodes, zero volume) */
+  CFEM_ERR_UNSUPPORTED = 7,
+  CFEM_ERR_IO = 8
+} cfem_status;
+
+/* Semantics of the numerical path. */
+typedef enum cfem_semantics {
+  CFEM_COMPAT = 0,     /* reproduce the reference's results, quirks included */
+  CFEM_CONSISTENT = 1  /* textbook operators, masses and loads */
+} cfem_semantics;
+
+typedef enum cfem_precision {
+  CFEM_FP64 = 0,         /* FP64 vectors and FP64 element operator */
+  CFEM_FP32 = 1,         /* FP32 vectors and operator, FP64 reductions */
+  CFEM_FP32_REFINE = 2   /* FP32 inner PCG inside FP64 iterative refinement */
+} cfem_precision;
+
+typedef enum cfem_stop_rule {
+  CFEM_STOP_REFERENCE = 0, /* gamma_new < tol * gamma0, gamma = r.M^-1.r (femfunc.cpp:92) */
+  CFEM_STOP_RESIDUAL = 1   /* ||r||_2 <= tol * ||f||_2 */
+} cfem_stop_rule;
+
+typedef enum cfem_matvec_form {
+  CFEM_FORM_AUTO = 0,      /* pick by measured bytes and time per element */
+  CFEM_FORM_GRADIENT = 1,  /* stored scaled shape gradients: K_e p = G^T D G p */
+  CFEM_FORM_STORED_KE = 2  /* stored 12x12 / 6x6 FP32 K_e (the reference's Klocals) */
+} cfem_matvec_form;
+
+typedef enum cfem_wavelet_type { CFEM_WAVELET_NONE = 0, CFEM_WAVELET_RICKER = 1, CFEM_WAVELET_BERLAGE = 2 } cfem_wavelet_type;
+
+/* The content of one prepared-mesh task (datakeeper.cpp:116-213). */
+typedef struct cfem_mesh {
+  int32_t dim;                   /* 2: CST triangles (plane stress), 3: linear tetrahedra */
+  int64_t n_nodes;
+  const double *nodes;           /* [n_nodes][dim] */
+  int64_t n_elems;
+  const int32_t *elems;          /* [n_elems][dim+1] 0-based node ids */
+  int64_t n_constraints;
+  const int32_t *constraints;    /* [n_constraints][2] node, Constraint::Type code (femstruct.h:39-52) */
+  int64_t n_loads;
+  const int32_t *load_nodes;     /* [n_loads] */
+  const double *load_vectors;    /* [n_loads][dim] */
+  int64_t n_faces;
+  const int32_t *face_nodes;     /* [n_faces][dim+1] dim face nodes, then the opposite node */
+  const int32_t *face_elems;     /* [n_faces] adjacent element */
+  const double *face_normals;    /* [n_faces][dim] as in stress.txt (normalised internally) */
+  const double *face_pressures;  /* [n_faces] */
+  const double *elem_young;      /* [n_elems] per-element Young's modulus, or NULL */
+} cfem_mesh;
+
+typedef struct cfem_material {
+  double young_modulus;  /* run_config youngModulus (default 2e7) */
+  double poisson_ratio;  /* run_config poissonRatio (default 0.3) */
+  double rho;            /* run_config rho (default 2400) */
+} cfem_material;
+
+typedef struct cfem_options {
+  int32_t semantics;     /* cfem_semantics */
+  int32_t matvec_form;   /* cfem_matvec_form */
+  int32_t patch_elems;   /* elements per CTA patch, 0 = autotuned */
+  int32_t verbose;       /* print PCG scalars like PRINT_DEBUG_INFO */
+} cfem_options;
+
+typedef struct cfem_wavelet {
+  int32_t type;          /* cfem_wavelet_type */
+  double freq, timeshift, ampl;
+} cfem_wavelet;
+
+typedef struct cfem_solve_params {
+  int32_t precision;     /* cfem_precision */
+  int32_t stop_rule;     /* cfem_stop_rule (inner rule for CFEM_FP32_REFINE) */
+  double tol;            /* reference: 1e-8 static, 1e-4 dynamics */
+  int32_t max_iter;      /* PCG iteration cap (per inner solve) */
+  double outer_tol;      /* CFEM_FP32_REFINE: stop when ||f - K x||_2 <= outer_tol ||f||_2 */
+  int32_t max_outer;     /* CFEM_FP32_REFINE: refinement step cap */
+} cfem_solve_params;
+
+typedef struct cfem_solve_info {
+  int32_t status;        /* cfem_status of the solve */
+  int32_t iterations;    /* total PCG iterations (all inner solves) */
+  int32_t outer_iterations;
+  double rel_residual;   /* ||f - K x||_2 / ||f||_2, FP64 true residual */
+  double gamma0, gamma;  /* first and last r.M^-1.r of the (last) PCG */
+  double solve_ms;       /* device time of the solve (CUDA events) */
+} cfem_solve_info;
+
+typedef struct cfem_dyn_params {
+  double beta1, beta2;   /* GN22 parameters; explicit when beta2 == 0 (femfunc.cpp:145) */
+  double dt, endtime;    /* steps = int(float(endtime) / float(dt)); endtime < 0: one relaxation step */
+  int32_t precision;     /* CFEM_FP64 or CFEM_FP32 */
+  double pcg_tol;        /* implicit: 1e-4 in compat (reference rule), else per stop_rule */
+  int32_t stop_rule;
+  int32_t max_iter;
+  int32_t warm_start;    /* implicit: start each PCG from the previous acceleration */
+  int32_t n_receivers;   /* optional trace recording: nodes and output buffer */
+  const int32_t *receiver_nodes;
+  double *receiver_trace; /* [steps][n_receivers][dim] displacements, host or device */
+} cfem_dyn_params;
+
+typedef struct cfem_dyn_info {
+  int32_t status;
+  int32_t steps;
+  int64_t pcg_iterations;
+  double solve_ms;
+} cfem_dyn_info;
+
+typedef struct cfem_ctx cfem_ctx;
+
+/* ---- lifetime ---------------------------------------------------------- */
+/* dataKeeper + ElementsData::setElementsData + genMask + calculateKlocals
+ * (datakeeper.cpp:246-252, fem_utils.cpp:41-51, cpu_fem_utils.cpp:182-520):
+ * uploads the mesh, renumbers it for locality, builds the DOF map, constraint
+ * masks, element operators and right-hand sides. `stream` is a cudaStream_t
+ * (NULL = legacy default stream). */
+CFEM_API cfem_status cfem_create(cfem_ctx **ctx, const cfem_mesh *mesh, const cfem_material *mat,
+                        const cfem_options *opt, void *stream);
+CFEM_API void cfem_destroy(cfem_ctx *ctx);
+CFEM_API const char *cfem_last_error_string(void);
+CFEM_API int32_t cfem_abi_version(void);
+CFEM_API cfem_status cfem_set_stream(cfem_ctx *ctx, void *stream);
+CFEM_API cfem_status cfem_synchronize(cfem_ctx *ctx);
+/* counts[0..5] = dim, n_nodes, n_elems, n_dof, n_patches, matvec_form */
+CFEM_API cfem_status cfem_get_counts(const cfem_ctx *ctx, int64_t *counts);
+
+/* ---- setup products, for bit-exact checks (host outputs) --------------- */
+/* genMask (cpu_fem_utils.cpp:182-213): mask[e*w + dim*a + d] = dim*elem[e][a] + d, w = 6(dim-1). */
+CFEM_API cfem_status cfem_dof_map(const cfem_ctx *ctx, int32_t *mask);
+/* genAdjElements (cpu_fem_utils.cpp:215-219): elements touching each DOF. */
+CFEM_API cfem_status cfem_adjacency(const cfem_ctx *ctx, int32_t *adj);
+/* ParseConstraints (datakeeper.cpp:139-171): 1 for every constrained DOF. */
+CFEM_API cfem_status cfem_bc_mask(const cfem_ctx *ctx, uint8_t *constrained);
+/* Locality renumbering: new->old node and element permutations. */
+CFEM_API cfem_status cfem_renumbering(const cfem_ctx *ctx, int32_t *node_new2old, int32_t *elem_new2old);
+/* calculateKlocals + applyConstraints (cpu_fem_utils.cpp:489-520): row-major
+ * w x w element matrices of elements [first, first+count) in the caller's order,
+ * rebuilt in FP64 from the stored operator. */
+CFEM_API cfem_status cfem_element_matrices(cfem_ctx *ctx, int64_t first, int64_t count, double *ke);
+/* Assembled diagonal of the constrained stiffness (getDiagonal + reduction). */
+CFEM_API cfem_status cfem_diagonal(cfem_ctx *ctx, double *diag);
+/* initFlocals / calcFlocals at time t, assembled (cpu_fem_utils.cpp:522-596). */
+CFEM_API cfem_status cfem_rhs(cfem_ctx *ctx, const cfem_wavelet *w, double t, double *f);
+
+/* ---- operators and solvers --------------------------------------------- */
+/* y = K' x, K' the constrained stiffness (Matrix::bmm + reductionWithMask,
+ * femfunc.cpp:66-67 then assembly). precision CFEM_FP64: double x, y;
+ * CFEM_FP32: float x, y. */
+CFEM_API cfem_status cfem_matvec(cfem_ctx *ctx, int32_t precision, const void *x, void *y);
+/* gpuPCG_EbE_vec (femfunc.cpp:25-128): Jacobi PCG for K' u = f from u = 0. */
+CFEM_API cfem_status cfem_pcg(cfem_ctx *ctx, const cfem_solve_params *prm, const double *f, double *u, cfem_solve_info *info);
+/* gpuCalculateFEM_EbE_vec (femfunc.cpp:3-23): static solve with the mesh's own loads. */
+CFEM_API cfem_status cfem_static_solve(cfem_ctx *ctx, const cfem_wavelet *w, const cfem_solve_params *prm, double *u,
+                              cfem_solve_info *info);
+/* gpuCalculateFEM_DYN (femfunc.cpp:130-381): GN22 time stepping, final displacements. */
+CFEM_API cfem_status cfem_dyn(cfem_ctx *ctx, const cfem_dyn_params *prm, const cfem_wavelet *w, double *u,
+                     cfem_dyn_info *info);
+/* k load cases at once: F, U are [k][n_dof] (RHS-major). The element operator
+ * is streamed once per matvec for all k. info may be NULL or [k]. */
+CFEM_API cfem_status cfem_pcg_multi(cfem_ctx *ctx, const cfem_solve_params *prm, int32_t k, const double *F, double *U,
+                           cfem_solve_info *info);
+/* Adjoint of the static solve K' u = f: lambda = K'^-1 dL/du, then
+ * dL/dE_e = -lambda_e^T (dK'_e/dE_e) u_e and dL/df = lambda. Outputs may be NULL. */
+CFEM_API cfem_status cfem_adjoint(cfem_ctx *ctx, const cfem_solve_params *prm, const double *u, const double *dLdu,
+                         double *dLdE, double *dLdf, cfem_solve_info *info);
+/* Per-element Young's modulus update (keeps geometry; rebuilds operator scale). */
+CFEM_API cfem_status cfem_set_young(cfem_ctx *ctx, const double *elem_young);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CFEM_H */

@@ -1,0 +1,218 @@
+"""GPU parity of the static path against the oracle and the reference fixtures.
+
+Tolerances: FP64 paths <= 1e-10 relative to the converged FP64 oracle (the
+spec bound); FP32 + FP64 refinement <= 1e-8; FP32-only results are held
+to FP32 accuracy. DOF map, adjacency, constraint masks and renumbering are
+bit-exact.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import STATIC_CASES, SYNTH_CASES, golden_problem, golden_ref, rel, GOLDEN
+from cudafemproject_gb300 import meshgen
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctxs():
+    from cudafemproject_gb300.solver import FemContext
+    cache = {}
+
+    def get(name, dim, semantics="compat", **kw):
+        key = (name, dim, semantics, tuple(sorted(kw.items())))
+        if key not in cache:
+            cache[key] = (FemContext(golden_problem(name, dim), semantics=semantics, **kw), golden_problem(name, dim))
+        return cache[key]
+    return get
+
+
+@pytest.mark.parametrize("name,dim", STATIC_CASES)
+def test_bit_exact_setup(ctxs, name, dim):
+    ctx, p = ctxs(name, dim)
+    o = O.Oracle(p)
+    assert np.array_equal(ctx.dof_map(), o.mask())
+    assert np.array_equal(ctx.adjacency(), o.adjacency())
+    assert np.array_equal(ctx.bc_mask(), o.bc())
+    n2o, e2o = ctx.renumbering()
+    assert np.array_equal(np.sort(n2o), np.arange(p.n_nodes))
+    assert np.array_equal(np.sort(e2o), np.arange(p.n_elems))
+    ref = golden_ref(f"static_{name}")
+    if "mask" in ref.files:
+        assert np.array_equal(ctx.dof_map().astype(np.float32), ref["mask"])
+        assert np.array_equal(ctx.adjacency().astype(np.float32), ref["adjElements"])
+
+
+def test_renumbering_deterministic(ctxs):
+    from cudafemproject_gb300.solver import FemContext
+    p = golden_problem("box4p", 3)
+    a = FemContext(p).renumbering()
+    b = FemContext(p).renumbering()
+    assert all(np.array_equal(x, y) for x, y in zip(a, b))
+
+
+@pytest.mark.parametrize("name,dim", STATIC_CASES)
+def test_element_matrices_and_diag(ctxs, name, dim):
+    ctx, p = ctxs(name, dim)
+    o = O.Oracle(p)
+    k = ctx.element_matrices()
+    ko = o.element_matrices()
+    assert rel(k, ko) < 1e-12
+    assert rel(ctx.diagonal(), o.diag()) < 1e-12
+    ref = golden_ref(f"static_{name}")
+    if "Klocals" in ref.files:  # the reference's FP32 Klocals (column-major per element)
+        w = 6 * (dim - 1)
+        kr = ref["Klocals"].reshape(-1, w, w).transpose(0, 2, 1)
+        assert rel(k, kr) < 2e-6
+
+
+@pytest.mark.parametrize("name,dim", STATIC_CASES)
+@pytest.mark.parametrize("semantics", ["compat", "consistent"])
+def test_rhs(ctxs, name, dim, semantics):
+    ctx, p = ctxs(name, dim, semantics)
+    o = O.Oracle(p, consistent=semantics == "consistent")
+    assert rel(ctx.rhs(), o.rhs()) < 1e-13
+    ref = golden_ref(f"static_{name}")
+    if semantics == "compat" and "Flocals" in ref.files:
+        # assembled reference Flocals
+        fl = np.zeros(p.n_dof)
+        np.add.at(fl, ref["mask"].astype(np.int64), ref["Flocals"].astype(np.float64))
+        assert rel(ctx.rhs(), fl) < 1e-6
+
+
+@pytest.mark.parametrize("name,dim", STATIC_CASES)
+def test_matvec(ctxs, name, dim):
+    ctx, p = ctxs(name, dim)
+    o = O.Oracle(p)
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal(p.n_dof)
+    assert rel(ctx.matvec(x, "fp64"), o.matvec(x)) < 1e-13
+    y32 = ctx.matvec(x.astype(np.float32), "fp32")
+    assert rel(y32, o.matvec(x.astype(np.float32).astype(np.float64))) < 2e-6
+
+
+@pytest.mark.parametrize("name,dim", STATIC_CASES)
+def test_static_fp64_reference_rule(ctxs, name, dim):
+    """Same algorithm and stopping rule as gpuPCG_EbE_vec (eps 1e-8 on gamma):
+    same iteration count as the FP64 oracle and the same iterate."""
+    ctx, p = ctxs(name, dim)
+    o = O.Oracle(p)
+    xo, ito = o.pcg(o.rhs(), tol=1e-8, rule=0)
+    u, info = ctx.static_solve("fp64", tol=1e-8, stop_rule="reference")
+    assert abs(info["iterations"] - ito) <= 1
+    assert rel(u, xo) < 1e-8
+    ref = golden_ref(f"static_{name}")
+    assert rel(u, ref["u"]) < 5e-4  # FP32 reference with the same loose stopping rule
+
+
+@pytest.mark.parametrize("name,dim", STATIC_CASES)
+def test_static_fp64_converged(ctxs, name, dim):
+    ctx, p = ctxs(name, dim)
+    o = O.Oracle(p)
+    xo, _ = o.static(tol=1e-14, rule=1)
+    u, info = ctx.static_solve("fp64", tol=1e-14, stop_rule="residual")
+    assert rel(u, xo) <= 1e-10
+    assert info["rel_residual"] < 1e-12
+
+
+@pytest.mark.parametrize("name,dim", STATIC_CASES)
+def test_static_fp32_refine(ctxs, name, dim):
+    ctx, p = ctxs(name, dim)
+    o = O.Oracle(p)
+    xo, _ = o.static(tol=1e-14, rule=1)
+    u, info = ctx.static_solve("fp32_refine", tol=1e-5, stop_rule="residual", outer_tol=1e-13)
+    assert rel(u, xo) <= 1e-8
+    assert info["outer_iterations"] >= 1
+
+
+@pytest.mark.parametrize("name,dim", STATIC_CASES)
+def test_static_fp32(ctxs, name, dim):
+    ctx, p = ctxs(name, dim)
+    o = O.Oracle(p)
+    xo, _ = o.static(tol=1e-14, rule=1)
+    u, info = ctx.static_solve("fp32", tol=1e-8, stop_rule="reference")
+    assert rel(u, xo) < 1e-3
+
+
+@pytest.mark.parametrize("name", ["test_rect_pcg", "9task_3"])
+def test_golden_vtk_gpu(ctxs, name):
+    ctx, p = ctxs(name, 2)
+    g = np.loadtxt(f"{GOLDEN}/{name}_vtk_displacements.txt")
+    u, _ = ctx.static_solve("fp32", tol=1e-8, stop_rule="reference")
+    assert rel(u, g) < 2e-5
+    u64, _ = ctx.static_solve("fp64", tol=1e-14, stop_rule="residual")
+    assert rel(u64, g) < 5e-6
+
+
+def test_square_2d_64_fp64_vs_oracle():
+    """The 64x64x2 CST configuration: FP64 Jacobi-PCG to relative residual 1e-12."""
+    from cudafemproject_gb300.solver import FemContext
+    p = meshgen.square_2d(64)
+    o = O.Oracle(p)
+    xo, _ = o.static(tol=1e-14, rule=1)
+    ctx = FemContext(p)
+    u, info = ctx.static_solve("fp64", tol=1e-12, stop_rule="residual")
+    assert info["rel_residual"] <= 1e-12
+    assert rel(u, xo) <= 1e-9
+    u2, _ = ctx.static_solve("fp64", tol=1e-14, stop_rule="residual")
+    assert rel(u2, xo) <= 1e-10
+
+
+def test_jittered_box_patch_sizes():
+    """Results do not depend on the CTA patch size (locality layout only)."""
+    from cudafemproject_gb300.solver import FemContext
+    p = meshgen.box_3d(6, 5, 14, jitter=0.2, seed=11)
+    o = O.Oracle(p)
+    xo, _ = o.static(tol=1e-14, rule=1)
+    for pe in (64, 256, 1024):
+        u, _ = FemContext(p, patch_elems=pe).static_solve("fp64", tol=1e-14, stop_rule="residual")
+        assert rel(u, xo) <= 1e-10, pe
+
+
+def test_consistent_static(ctxs):
+    ctx, p = ctxs("box4p", 3, "consistent")
+    o = O.Oracle(p, consistent=True)
+    xo, _ = o.static(tol=1e-14, rule=1)
+    u, _ = ctx.static_solve("fp64", tol=1e-14, stop_rule="residual")
+    assert rel(u, xo) <= 1e-10
+
+
+def test_pcg_explicit_rhs_and_torch_device_pointers(ctxs):
+    torch = pytest.importorskip("torch")
+    ctx, p = ctxs("box3", 3)
+    o = O.Oracle(p)
+    f = np.random.default_rng(5).standard_normal(p.n_dof)
+    xo, _ = o.pcg(f, tol=1e-14, rule=1)
+    u, info = ctx.pcg(f, "fp64", tol=1e-14, stop_rule="residual")
+    assert rel(u, xo) <= 1e-10
+    fd = torch.tensor(f, device="cuda")
+    ud, _ = ctx.pcg(fd, "fp64", tol=1e-14, stop_rule="residual")
+    assert rel(ud.cpu().numpy(), xo) <= 1e-10
+
+
+def test_error_paths():
+    from cudafemproject_gb300 import capi
+    from cudafemproject_gb300.solver import FemContext
+    p = golden_problem("sq8", 2)
+    bad = golden_problem("sq8", 2)
+    bad.nodes = np.vstack([bad.nodes, [[5.0, 5.0]]])  # unused node
+    with pytest.raises(capi.CfemError) as e:
+        FemContext(bad)
+    assert e.value.status == capi.ERR_MESH
+    flat = golden_problem("sq8", 2)
+    flat.nodes = flat.nodes.copy()
+    flat.nodes[:, 1] = 0.0  # zero-area elements
+    with pytest.raises(capi.CfemError) as e:
+        FemContext(flat)
+    assert e.value.status == capi.ERR_MESH
+    ctx = FemContext(p)
+    f = np.full(p.n_dof, np.nan)
+    with pytest.raises(capi.CfemError) as e:
+        ctx.pcg(f, "fp64")
+    assert e.value.status == capi.ERR_DIVERGED
+    u, info = ctx.pcg(np.ones(p.n_dof), "fp64", tol=1e-30, stop_rule="residual", max_iter=3, allow_not_converged=True)
+    assert info["status"] == capi.ERR_NOT_CONVERGED and info["iterations"] == 3
+    # the context stays usable after the failures
+    u, info = ctx.static_solve("fp64", tol=1e-12, stop_rule="residual")
+    assert info["status"] == 0

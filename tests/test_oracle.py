@@ -1,0 +1,95 @@
+"""The oracle (oracle/fem_oracle.c) pinned against the reference's own outputs.
+
+* FP32 element-local port == reference CPU build, bit for bit (fixtures made by
+  tests/golden/make_golden.py from the unmodified reference sources);
+* reference golden VTKs (testing/*_test/results.vtk);
+* FP64 port == FP64 global form (same mathematics, different summation order).
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import DYN_CASES, STATIC_CASES, SYNTH_CASES, dyn_case, golden_problem, golden_ref, rel, GOLDEN
+
+
+@pytest.mark.parametrize("name,dim", STATIC_CASES)
+def test_port_f32_bit_exact_static(name, dim):
+    p = golden_problem(name, dim)
+    ref = golden_ref(f"static_{name}")
+    u, it = O.ebe_static(p)
+    assert it == int(ref["iterations"])
+    assert np.array_equal(u, ref["u"])
+
+
+@pytest.mark.parametrize("name,dim", SYNTH_CASES)
+def test_port_f32_setup_arrays_bit_exact(name, dim):
+    p = golden_problem(name, dim)
+    ref = golden_ref(f"static_{name}")
+    s = O.ebe_setup(p)
+    assert np.array_equal(s["mask"], ref["mask"])
+    assert np.array_equal(s["adj"], ref["adjElements"])
+    assert np.array_equal(s["diagK"], ref["diagK"])
+    assert np.array_equal(s["Flocals"], ref["Flocals"])
+    assert np.array_equal(s["areas"], ref["areas"])
+    if "Klocals" in ref.files:
+        assert np.array_equal(s["Klocals"], ref["Klocals"])
+
+
+@pytest.mark.parametrize("name", DYN_CASES)
+def test_port_f32_bit_exact_dynamics(name):
+    p, w, args, ref = dyn_case(name)
+    u, steps, its = O.ebe_dyn(p, *args, wavelet=w)
+    assert its == int(ref["pcg_iterations"])
+    assert np.array_equal(u, ref["u"])
+
+
+@pytest.mark.parametrize("name", ["test_rect_pcg", "9task_3"])
+def test_golden_vtk(name):
+    p = golden_problem(name, 2)
+    g = np.loadtxt(f"{GOLDEN}/{name}_vtk_displacements.txt")
+    u32, _ = O.ebe_static(p)
+    assert rel(u32, g) < 3e-6  # the VTK holds 6 significant digits
+    o = O.Oracle(p)
+    x, _ = o.static(tol=1e-14, rule=1)
+    assert rel(x, g) < 5e-6
+
+
+@pytest.mark.parametrize("name,dim", STATIC_CASES)
+def test_port_f64_equals_global_form(name, dim):
+    p = golden_problem(name, dim)
+    u64, it = O.ebe_static(p, f64=True)
+    o = O.Oracle(p)
+    x, it2 = o.pcg(o.rhs(), tol=1e-8, rule=0)
+    assert abs(it - it2) <= 1
+    x2, _ = o.static(tol=1e-14, rule=1)
+    assert rel(x2, O.ebe_static(p, eps=1e-30, f64=True)[0]) < 1e-9
+
+
+@pytest.mark.parametrize("name", DYN_CASES)
+def test_dyn_f64_port_equals_global_form(name):
+    p, w, args, ref = dyn_case(name)
+    u64, steps, its = O.ebe_dyn(p, *args, wavelet=w, f64=True)
+    o = O.Oracle(p)
+    ug, steps2, its2 = o.dyn(*args, wavelet=w)
+    assert steps == steps2
+    assert rel(ug, u64) < 5e-6  # implicit: both stop PCG at gamma < 1e-4 gamma0
+    assert rel(ug, ref["u"]) < 1e-4
+
+
+def test_oracle_bc_decode_q6():
+    """Constraint codes UX=1, UY=2, UZ=3 decoded with &UX, &UY, &UZ (datakeeper.cpp:153-163)."""
+    from cudafemproject_gb300 import meshgen
+    p = meshgen.box_3d(1, 1, 1, traction=None)
+    p.cons = np.array([[0, 1], [1, 2], [2, 3], [3, 4], [4, 5], [5, 6], [6, 7]], np.int32)
+    b = O.Oracle(p).bc().reshape(-1, 3)
+    expect = {1: [1, 0, 1], 2: [0, 1, 1], 3: [1, 1, 1], 4: [0, 0, 0], 5: [1, 0, 1], 6: [0, 1, 1], 7: [1, 1, 1]}
+    for node, code in p.cons:
+        assert b[node].tolist() == expect[int(code)], (node, code)
+
+
+def test_consistent_traction_total_force():
+    from cudafemproject_gb300 import meshgen
+    p = meshgen.box_3d(3, 3, 6, traction=(0.0, -1e3, 0.0))
+    f = O.Oracle(p, consistent=True).rhs().reshape(-1, 3)
+    assert abs(f[:, 1].sum() - (-1e3 * 1.0 * 1.0)) < 1e-6
+    assert abs(f[:, 0].sum()) < 1e-9
