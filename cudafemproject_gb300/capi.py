@@ -53,7 +53,7 @@ class SolveParams(C.Structure):
 
 class SolveInfo(C.Structure):
     _fields_ = [("status", i32), ("iterations", i32), ("outer_iterations", i32), ("rel_residual", f64),
-                ("gamma0", f64), ("gamma", f64), ("solve_ms", f64)]
+                ("gamma0", f64), ("gamma", f64), ("solve_ms", f64), ("kernel_launches", i64)]
 
 
 class DynParams(C.Structure):
@@ -89,6 +89,8 @@ SIGNATURES = [
     ("cfem_pcg_multi", i32, [vp, C.POINTER(SolveParams), i32, vp, vp, C.POINTER(SolveInfo)]),
     ("cfem_adjoint", i32, [vp, C.POINTER(SolveParams), vp, vp, vp, vp, C.POINTER(SolveInfo)]),
     ("cfem_set_young", i32, [vp, vp]),
+    ("cfem_profile_matvec", i32, [vp, i32, i32, C.POINTER(f64), C.POINTER(f64)]),
+    ("cfem_run_task", i32, [C.c_char_p, C.c_char_p, i32, vp, i64, C.POINTER(SolveInfo), C.POINTER(DynInfo)]),
 ]
 
 _lib = None

@@ -47,6 +47,7 @@ void launch_mv_t(cfem_ctx *c, int mode, const MvParams<T> &P) {
     else k_matvec<T, 2, MV_DYN><<<g, b, smem, c->stream>>>(P);
   }
   CKL();
+  c->launches += 1;
 }
 
 template <typename T>
@@ -66,6 +67,7 @@ void launch_init(cfem_ctx *c, const VecParams<T> &P, int warm) {
   if (c->dim == 3) k_pcg_init<T, 3><<<c->grid_vec, kThreads, 0, c->stream>>>(P, warm);
   else k_pcg_init<T, 2><<<c->grid_vec, kThreads, 0, c->stream>>>(P, warm);
   CKL();
+  c->launches += 1;
 }
 
 template <typename T>
@@ -73,6 +75,7 @@ void launch_update(cfem_ctx *c, const VecParams<T> &P) {
   if (c->dim == 3) k_pcg_update<T, 3><<<c->grid_vec, kThreads, 0, c->stream>>>(P);
   else k_pcg_update<T, 2><<<c->grid_vec, kThreads, 0, c->stream>>>(P);
   CKL();
+  c->launches += 1;
 }
 
 // Jacobi PCG on A x = V.f with A = cM*M + cK*K' (mcoef selects the mass term).
@@ -102,19 +105,29 @@ PcgResult run_pcg_t(cfem_ctx *c, Vecs<T> &V, T cK, T cM, const T *mcoef, int war
   if (!gc.exec || gc.key0 != (const void *)mcoef || gc.key1 != (double)cK || gc.key2 != (double)cM) {
     gc.reset();
     cudaGraph_t graph;
+    const int64_t launches_before_capture = c->launches;
     CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    for (int it = 0; it < c->chunk; ++it) {
-      T *pold = (it & 1) ? V.pB.p : V.pA.p;
-      T *pnew = (it & 1) ? V.pA.p : V.pB.p;
-      MvParams<T> m = mv;
-      m.x = V.z.p;
-      m.x2 = pold;
-      m.xout = pnew;
-      m.y = V.u.p;
-      launch_mv<T>(c, MV_PCG, m);
-      launch_update<T>(c, vec_params<T>(c, V, pnew, sc));
+    try {
+      for (int it = 0; it < c->chunk; ++it) {
+        T *pold = (it & 1) ? V.pB.p : V.pA.p;
+        T *pnew = (it & 1) ? V.pA.p : V.pB.p;
+        MvParams<T> m = mv;
+        m.x = V.z.p;
+        m.x2 = pold;
+        m.xout = pnew;
+        m.y = V.u.p;
+        launch_mv<T>(c, MV_PCG, m);
+        launch_update<T>(c, vec_params<T>(c, V, pnew, sc));
+      }
+    } catch (...) {
+      cudaGraph_t broken = nullptr;
+      cudaStreamEndCapture(c->stream, &broken);
+      if (broken) cudaGraphDestroy(broken);
+      (void)cudaGetLastError();
+      throw;
     }
     CK(cudaStreamEndCapture(c->stream, &graph));
+    c->launches = launches_before_capture;
     CK(cudaGraphInstantiate(&gc.exec, graph, 0));
     cudaGraphDestroy(graph);
     gc.key0 = mcoef;
@@ -130,6 +143,7 @@ PcgResult run_pcg_t(cfem_ctx *c, Vecs<T> &V, T cK, T cM, const T *mcoef, int war
     if (launch > max_launches || stalled > 4)
       throw Fail{CFEM_ERR_CUDA, "PCG recurrence stopped advancing on the device"};
     CK(cudaGraphLaunch(gc.exec, c->stream));
+    c->launches += 2 * c->chunk;
     CK(cudaMemcpyAsync(c->h_sc, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     if (c->verbose)
@@ -219,6 +233,7 @@ void set_diag_vectors(cfem_ctx *c, const double *diagA64) {
 // Static-type solve of K' x = f (f internal FP64 in c->v64.f). Result in c->v64.x.
 cfem_status solve_internal(cfem_ctx *c, const cfem_solve_params *prm, cfem_solve_info *info) {
   cfem_solve_info inf{};
+  c->launches = 0;
   set_diag_vectors(c, c->diagK.p);
   CK(cudaEventRecord(c->ev0, c->stream));
   const int prec = prm->precision;
@@ -271,6 +286,7 @@ cfem_status solve_internal(cfem_ctx *c, const cfem_solve_params *prm, cfem_solve
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
   inf.solve_ms = ms;
+  inf.kernel_launches = c->launches;
   double rr = 0, ff = 0;
   true_residual(c, c->v64.f.p, c->v64.x.p, c->tmp64b.p, nullptr, rr, ff);
   inf.rel_residual = ff > 0 ? std::sqrt(rr / ff) : std::sqrt(rr);
@@ -289,6 +305,7 @@ void make_rhs(cfem_ctx *c, double a, double b, double *dst) {
 
 // ======================================================================== C-ABI
 cfem_status run_guarded(const std::function<cfem_status()> &fn) {
+  (void)cudaGetLastError();  // a failure of an earlier call must not leak into this one
   try {
     return fn();
   } catch (const Fail &f) {
@@ -503,6 +520,33 @@ void rebuild_operator(cfem_ctx *c) {
   if (herr) throw Fail{CFEM_ERR_MESH, "an element has zero or non-finite volume"};
 }
 
+void enter(cfem_ctx *c) {
+  if (c->own_stream) {
+    CK(cudaEventRecord(c->ev_in, c->user_stream));
+    CK(cudaStreamWaitEvent(c->stream, c->ev_in, 0));
+  }
+}
+
+// The legacy default stream cannot be captured into a CUDA graph; a context
+// given it (or NULL) issues its work on a stream of its own and orders that
+// stream after the caller's at every entry point that reads caller memory.
+void attach_stream(cfem_ctx *c, cudaStream_t s) {
+  if (c->own_stream && c->stream) {
+    CK(cudaStreamSynchronize(c->stream));
+    cudaStreamDestroy(c->stream);
+    c->stream = nullptr;
+    c->own_stream = false;
+  }
+  c->user_stream = s;
+  if (s == nullptr || s == cudaStreamLegacy || s == cudaStreamPerThread) {
+    CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    c->own_stream = true;
+    if (!c->ev_in) CK(cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming));
+  } else {
+    c->stream = s;
+  }
+}
+
 void check_ctx(const cfem_ctx *c) {
   if (!c) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "null context"};
 }
@@ -527,6 +571,9 @@ int32_t cfem_abi_version(void) { return CFEM_ABI_VERSION; }
 
 const char *cfem_last_error_string(void) { return g_last_error.c_str(); }
 
+// used by the C++ host layer (femfunc.cpp) to report its own failures
+void cfem_set_error_string(const char *msg) { g_last_error = msg ? msg : ""; }
+
 cfem_status cfem_create(cfem_ctx **out, const cfem_mesh *mesh, const cfem_material *mat, const cfem_options *opt,
                         void *stream) {
   return run_guarded([&]() -> cfem_status {
@@ -537,7 +584,7 @@ cfem_status cfem_create(cfem_ctx **out, const cfem_mesh *mesh, const cfem_materi
         (mesh->n_faces > 0 && (!mesh->face_nodes || !mesh->face_elems || !mesh->face_normals || !mesh->face_pressures)))
       throw Fail{CFEM_ERR_INVALID_ARGUMENT, "mesh count given without its array"};
     std::unique_ptr<cfem_ctx> c(new cfem_ctx());
-    c->stream = (cudaStream_t)stream;
+    attach_stream(c.get(), (cudaStream_t)stream);
     setup_context(c.get(), mesh, mat, opt);
     *out = c.release();
     return CFEM_OK;
@@ -554,7 +601,7 @@ cfem_status cfem_set_stream(cfem_ctx *ctx, void *stream) {
   return run_guarded([&]() -> cfem_status {
     check_ctx(ctx);
     CK(cudaStreamSynchronize(ctx->stream));
-    ctx->stream = (cudaStream_t)stream;
+    attach_stream(ctx, (cudaStream_t)stream);
     ctx->graph64.reset();
     ctx->graph32.reset();
     return CFEM_OK;
@@ -688,6 +735,7 @@ cfem_status cfem_rhs(cfem_ctx *ctx, const cfem_wavelet *w, double t, double *f) 
 cfem_status cfem_matvec(cfem_ctx *ctx, int32_t precision, const void *x, void *y) {
   return run_guarded([&]() -> cfem_status {
     check_ctx(ctx);
+    enter(ctx);
     if (!x || !y) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "null vector"};
     if (precision == CFEM_FP64) {
       to_internal<double>(ctx, (const double *)x, ctx->v64.z.p);
@@ -731,6 +779,7 @@ cfem_status cfem_matvec(cfem_ctx *ctx, int32_t precision, const void *x, void *y
 cfem_status cfem_pcg(cfem_ctx *ctx, const cfem_solve_params *prm, const double *f, double *u, cfem_solve_info *info) {
   return run_guarded([&]() -> cfem_status {
     check_ctx(ctx);
+    enter(ctx);
     if (!f || !u) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "null vector"};
     cfem_solve_params p = prm ? *prm : default_params();
     to_internal<double>(ctx, f, ctx->v64.f.p);
@@ -758,6 +807,58 @@ cfem_status cfem_static_solve(cfem_ctx *ctx, const cfem_wavelet *w, const cfem_s
     to_caller<double>(ctx, ctx->v64.x.p, u);
     CK(cudaStreamSynchronize(ctx->stream));
     return st;
+  });
+}
+
+cfem_status cfem_profile_matvec(cfem_ctx *ctx, int32_t precision, int32_t n_launches, double *ms_per_launch,
+                                double *bytes_per_launch) {
+  return run_guarded([&]() -> cfem_status {
+    check_ctx(ctx);
+    if (n_launches <= 0) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "n_launches must be positive"};
+    // scalars that make the kernel take its full path: iteration > 0, beta = 1
+    Scalars h{};
+    h.iter = 1;
+    h.gamma = h.gamma_prev = 1.0;
+    Scalars *sc = ctx->sc.p + 2;
+    CK(cudaMemcpyAsync(sc, &h, sizeof(Scalars), cudaMemcpyHostToDevice, ctx->stream));
+    const size_t ts = precision == CFEM_FP64 ? 8 : 4;
+    auto run = [&](int n) {
+      for (int i = 0; i < n; ++i) {
+        if (precision == CFEM_FP64) {
+          MvParams<double> mv = base_mv<double>(ctx);
+          mv.diagA = ctx->v64.diagA.p;
+          mv.sc = sc;
+          mv.x = ctx->v64.z.p;
+          mv.x2 = (i & 1) ? ctx->v64.pB.p : ctx->v64.pA.p;
+          mv.xout = (i & 1) ? ctx->v64.pA.p : ctx->v64.pB.p;
+          mv.y = ctx->v64.u.p;
+          launch_mv<double>(ctx, MV_PCG, mv);
+        } else {
+          MvParams<float> mv = base_mv<float>(ctx);
+          mv.diagA = ctx->v32.diagA.p;
+          mv.sc = sc;
+          mv.x = ctx->v32.z.p;
+          mv.x2 = (i & 1) ? ctx->v32.pB.p : ctx->v32.pA.p;
+          mv.xout = (i & 1) ? ctx->v32.pA.p : ctx->v32.pB.p;
+          mv.y = ctx->v32.u.p;
+          launch_mv<float>(ctx, MV_PCG, mv);
+        }
+      }
+    };
+    run(3);  // warm-up
+    CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    run(n_launches);
+    CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    CK(cudaEventSynchronize(ctx->ev1));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    if (ms_per_launch) *ms_per_launch = ms / n_launches;
+    if (bytes_per_launch)
+      *bytes_per_launch = (double)ctx->ne * (ctx->ncomp * ts + 8) + (double)ctx->nn * ctx->vw * ts * 4;
+    // leave the work vectors clean for the next solve
+    if (precision == CFEM_FP64) ctx->v64.u.zero(ctx->stream); else ctx->v32.u.zero(ctx->stream);
+    CK(cudaStreamSynchronize(ctx->stream));
+    return CFEM_OK;
   });
 }
 

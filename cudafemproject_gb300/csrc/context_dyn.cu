@@ -247,8 +247,16 @@ cfem_status run_dyn(cfem_ctx *c, const cfem_dyn_params *prm, const cfem_wavelet 
     if (pairs > 0) {
       cudaGraph_t g;
       CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-      one_step(d0.p, d1.p);
-      one_step(d1.p, d0.p);
+      try {
+        one_step(d0.p, d1.p);
+        one_step(d1.p, d0.p);
+      } catch (...) {
+        cudaGraph_t broken = nullptr;
+        cudaStreamEndCapture(c->stream, &broken);
+        if (broken) cudaGraphDestroy(broken);
+        (void)cudaGetLastError();
+        throw;
+      }
       CK(cudaStreamEndCapture(c->stream, &g));
       CK(cudaGraphInstantiate(&exec, g, 0));
       cudaGraphDestroy(g);
@@ -310,6 +318,7 @@ extern "C" {
 cfem_status cfem_dyn(cfem_ctx *ctx, const cfem_dyn_params *prm, const cfem_wavelet *w, double *u, cfem_dyn_info *info) {
   return run_guarded([&]() -> cfem_status {
     check_ctx(ctx);
+    enter(ctx);
     if (!prm || !u) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "null argument"};
     if (prm->precision == CFEM_FP64) return run_dyn<double>(ctx, prm, w, u, info, ctx->elems_caller.data());
     if (prm->precision == CFEM_FP32) return run_dyn<float>(ctx, prm, w, u, info, ctx->elems_caller.data());
@@ -321,6 +330,7 @@ cfem_status cfem_pcg_multi(cfem_ctx *ctx, const cfem_solve_params *prm, int32_t 
                            cfem_solve_info *info) {
   return run_guarded([&]() -> cfem_status {
     check_ctx(ctx);
+    enter(ctx);
     if (k <= 0 || !F || !U) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "bad multi-RHS arguments"};
     cfem_solve_params p = prm ? *prm : default_params();
     cfem_status worst = CFEM_OK;
@@ -341,6 +351,7 @@ cfem_status cfem_adjoint(cfem_ctx *ctx, const cfem_solve_params *prm, const doub
                          double *dLdf, cfem_solve_info *info) {
   return run_guarded([&]() -> cfem_status {
     check_ctx(ctx);
+    enter(ctx);
     if (!u || !dLdu) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "null input"};
     cfem_solve_params p = prm ? *prm : default_params();
     // lambda = K'^-1 dL/du (K' symmetric)
@@ -377,6 +388,7 @@ cfem_status cfem_adjoint(cfem_ctx *ctx, const cfem_solve_params *prm, const doub
 cfem_status cfem_set_young(cfem_ctx *ctx, const double *elem_young) {
   return run_guarded([&]() -> cfem_status {
     check_ctx(ctx);
+    enter(ctx);
     if (!elem_young) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "null array"};
     std::vector<double> yv(ctx->ne);
     CK(cudaMemcpy(yv.data(), elem_young, sizeof(double) * ctx->ne, cudaMemcpyDefault));

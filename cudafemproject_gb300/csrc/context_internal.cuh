@@ -89,7 +89,10 @@ using namespace cfem;
 using namespace cfem::detail;
 
 struct cfem_ctx {
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;       // the stream all work is issued on (capturable)
+  cudaStream_t user_stream = nullptr;  // the caller's stream; work is ordered after it
+  bool own_stream = false;
+  cudaEvent_t ev_in = nullptr;
   int device = 0, n_sm = 0;
   int dim = 0, nv = 0, w = 0, vw = 0, ncomp = 0;
   int64_t nn = 0, ne = 0, nd = 0, nvec = 0;
@@ -124,6 +127,7 @@ struct cfem_ctx {
   int grid_mv = 0, grid_vec = 0;
   size_t smem64 = 0, smem32 = 0;
   int chunk = 16;
+  int64_t launches = 0;  // kernels issued since the counter was last reset
   GraphCache graph64, graph32;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   // reference re-sorting quirk (compat dynamics)
@@ -138,6 +142,8 @@ struct cfem_ctx {
     if (h_rr) cudaFreeHost(h_rr);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
+    if (ev_in) cudaEventDestroy(ev_in);
+    if (own_stream && stream) cudaStreamDestroy(stream);
   }
 };
 
@@ -168,6 +174,8 @@ void true_residual(cfem_ctx *c, const double *f, const double *x, double *r, flo
 void make_rhs(cfem_ctx *c, double a, double b, double *dst);
 cfem_status run_guarded(const std::function<cfem_status()> &fn);
 void check_ctx(const cfem_ctx *c);
+// Orders the context's stream after the caller's stream (device inputs written there).
+void enter(cfem_ctx *c);
 cfem_solve_params default_params();
 cfem_status solve_internal(cfem_ctx *c, const cfem_solve_params *prm, cfem_solve_info *info);
 void rebuild_operator(cfem_ctx *c);

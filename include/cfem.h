@@ -132,6 +132,7 @@ typedef struct cfem_solve_info {
   double rel_residual;   /* ||f - K x||_2 / ||f||_2, FP64 true residual */
   double gamma0, gamma;  /* first and last r.M^-1.r of the (last) PCG */
   double solve_ms;       /* device time of the solve (CUDA events) */
+  int64_t kernel_launches; /* kernels issued by the solve (graph nodes included) */
 } cfem_solve_info;
 
 typedef struct cfem_dyn_params {
@@ -211,6 +212,20 @@ CFEM_API cfem_status cfem_pcg_multi(cfem_ctx *ctx, const cfem_solve_params *prm,
  * dL/dE_e = -lambda_e^T (dK'_e/dE_e) u_e and dL/df = lambda. Outputs may be NULL. */
 CFEM_API cfem_status cfem_adjoint(cfem_ctx *ctx, const cfem_solve_params *prm, const double *u, const double *dLdu,
                          double *dLdE, double *dLdf, cfem_solve_info *info);
+/* The whole reference flow for one task of a run_config file (main.cpp:18-33
+ * with argv): read the config and the prepared mesh, run the static or dynamic
+ * solve per task_type, optionally write results.vtk (VTKfile.cpp:281-386) into
+ * <working_path>/fem_results/<DIM>D/<task>/. u_out (n_out doubles, may be NULL)
+ * receives the displacements. Keys under "gb300" select precision/semantics. */
+CFEM_API cfem_status cfem_run_task(const char *config_path, const char *task, int32_t write_vtk, double *u_out,
+                                   int64_t n_out, cfem_solve_info *static_info, cfem_dyn_info *dyn_info);
+/* Measurement: n back-to-back launches of the PCG-form matvec kernel (direction
+ * update + element operator + scatter + p.Ap reduction) on the context's stream,
+ * timed with CUDA events. Returns the mean device time per launch and the
+ * algorithmic DRAM bytes of one launch: per element the stored operator and
+ * local connectivity, per node z and p read, p written, y accumulated. */
+CFEM_API cfem_status cfem_profile_matvec(cfem_ctx *ctx, int32_t precision, int32_t n_launches, double *ms_per_launch,
+                                         double *bytes_per_launch);
 /* Per-element Young's modulus update (keeps geometry; rebuilds operator scale). */
 CFEM_API cfem_status cfem_set_young(cfem_ctx *ctx, const double *elem_young);
 

@@ -1,0 +1,73 @@
+"""Adjoint sensitivities and multi-RHS solves against the FP64 oracle."""
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import rel
+from cudafemproject_gb300 import meshgen
+
+pytestmark = pytest.mark.gpu
+
+
+def _problem(seed=3):
+    p = meshgen.box_3d(3, 3, 9, jitter=0.15, seed=seed, traction=(0.0, -1e3, 0.0))
+    rng = np.random.default_rng(seed)
+    p.elem_E = 2e7 * np.exp(0.5 * rng.standard_normal(p.n_elems))
+    return p
+
+
+def test_grad_young_vs_oracle_and_fd():
+    from cudafemproject_gb300.solver import FemContext
+    p = _problem()
+    ctx = FemContext(p, semantics="consistent")
+    o = O.Oracle(p, consistent=True)
+    u, _ = ctx.static_solve("fp64", tol=1e-14, stop_rule="residual")
+    u = u.ravel()
+    f = ctx.rhs()
+    # compliance L = f.u  ->  dL/du = f
+    dE, df, info = ctx.adjoint(u, f)
+    lam, _ = o.pcg(f, tol=1e-14, rule=1)
+    g_or = o.grad_E(lam, u)
+    assert rel(dE, g_or) <= 1e-6
+    assert rel(df, lam) <= 1e-9
+    # central finite differences on a few elements (step 1e-4 relative)
+    rng = np.random.default_rng(0)
+    for e in rng.choice(p.n_elems, 5, replace=False):
+        vals = []
+        for s in (+1, -1):
+            q = _problem()
+            q.elem_E = q.elem_E.copy()
+            q.elem_E[e] *= 1 + s * 1e-4
+            c2 = FemContext(q, semantics="consistent")
+            u2, _ = c2.static_solve("fp64", tol=1e-14, stop_rule="residual")
+            vals.append(f @ u2.ravel())
+        fd = (vals[0] - vals[1]) / (2e-4 * p.elem_E[e])
+        assert abs(fd - dE[e]) <= 1e-4 * abs(dE[e]) + 1e-20, (e, fd, dE[e])
+
+
+def test_set_young_matches_fresh_context():
+    from cudafemproject_gb300.solver import FemContext
+    p = _problem()
+    ctx = FemContext(p, semantics="consistent")
+    y2 = p.elem_E * 1.5
+    ctx.set_young(y2)
+    q = _problem()
+    q.elem_E = y2
+    u1, _ = ctx.static_solve("fp64", tol=1e-14, stop_rule="residual")
+    u2, _ = FemContext(q, semantics="consistent").static_solve("fp64", tol=1e-14, stop_rule="residual")
+    assert rel(u1, u2) < 1e-12
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("fp32_refine", 1e-8)])
+def test_multi_rhs(precision, tol):
+    from cudafemproject_gb300.solver import FemContext
+    p = meshgen.box_3d(3, 3, 9, jitter=0.2, seed=1)
+    o = O.Oracle(p)
+    rng = np.random.default_rng(7)
+    F = rng.standard_normal((5, p.n_dof))
+    ctx = FemContext(p)
+    U, infos = ctx.pcg_multi(F, precision=precision, tol=1e-14 if precision == "fp64" else 1e-5,
+                             stop_rule="residual", outer_tol=1e-13)
+    for i in range(5):
+        x, _ = o.pcg(F[i], tol=1e-14, rule=1)
+        assert rel(U[i], x) <= tol
