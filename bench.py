@@ -9,7 +9,8 @@ Workload (one step = one full static solve, inputs resident in HBM): box
 1,390,179 DOF), interior nodes jittered +-0.2h (seed 0), E=2e7, nu=0.25, z=0
 clamped, traction 1e3 in -y on z=4, textbook (consistent) traction loads.
 The target error is measured against an FP64 solution converged to relative
-residual 1e-14 before timing. L2 is flushed (512 MB write) before every step.
+residual 1e-13 before timing; each method's stopping tolerance is calibrated (untimed) to the
+loosest value that reaches the target. L2 is flushed (512 MB write) before every step.
 The path does not shard (one mesh, one GPU): with N > 1 every rank solves its
 own replica and `value` is the max-over-ranks time of a replica's solve.
 """
@@ -178,7 +179,7 @@ def main():
     nd = p.n_dof
     f_host = ctx.rhs()
     # FP64 reference solution (untimed): plain FP64 PCG to rel. residual 1e-15
-    x_ref, inf_ref = ctx.pcg(f_host, "fp64", tol=1e-14, stop_rule="residual", max_iter=30000,
+    x_ref, inf_ref = ctx.pcg(f_host, "fp64", tol=1e-13, stop_rule="residual", max_iter=30000,
                              allow_not_converged=True)
     xr = np.asarray(x_ref)
     nref = np.linalg.norm(xr)
@@ -191,18 +192,32 @@ def main():
     u_dev = torch.zeros(nd, dtype=torch.float64, device="cuda")
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
-    refine = dict(precision="fp32_refine", tol=1e-4, stop_rule="residual", outer_tol=1e-12, max_outer=30,
-                  max_iter=30000)
-    plain64 = dict(precision="fp64", tol=1e-12, stop_rule="residual", max_iter=30000)
-
     def solve(kw, f=f_dev, out=u_dev):
-        return ctx.pcg(f, out=out, **kw)
+        return ctx.pcg(f, out=out, allow_not_converged=True, **kw)
 
-    # calibrate: both methods must reach the target error
-    _, inf32 = solve(refine)
-    e32 = err(u_dev.cpu().numpy())
-    _, inf64 = solve(plain64)
-    e64 = err(u_dev.cpu().numpy())
+    # Calibration (untimed): for each method the loosest stopping tolerance
+    # whose answer is within TARGET_ERR of the FP64 reference solution.
+    plain64 = None
+    for tol in (1e-7, 1e-8, 1e-9, 1e-10, 1e-11, 1e-12):
+        kw = dict(precision="fp64", tol=tol, stop_rule="residual", max_iter=30000)
+        _, i64 = solve(kw)
+        e64 = err(u_dev.cpu().numpy())
+        if e64 <= TARGET_ERR:
+            plain64 = kw
+            break
+    refine, best = None, None
+    for inner in (1e-3, 1e-4):
+        for outer in (1e-6, 1e-7, 1e-8, 1e-9, 1e-10):
+            kw = dict(precision="fp32_refine", tol=inner, stop_rule="residual", outer_tol=outer, max_outer=30,
+                      max_iter=30000)
+            _, i32 = solve(kw)
+            e32 = err(u_dev.cpu().numpy())
+            if e32 <= TARGET_ERR:
+                if best is None or i32["solve_ms"] < best:
+                    refine, best = kw, i32["solve_ms"]
+                break
+    if refine is None or plain64 is None:
+        raise SystemExit(f"calibration failed to reach {TARGET_ERR}: refine={refine} fp64={plain64}")
     for _ in range(args.warmup):
         solve(refine)
     torch.cuda.synchronize()
@@ -233,6 +248,7 @@ def main():
         _, i64 = solve(plain64)
         t64.append(i64["solve_ms"])
     ms64 = float(np.mean(t64))
+    e64_timed = err(u_dev.cpu().numpy())
     # e2e through the C-ABI with host buffers (h2d of f, d2h of u inside the timed region)
     u_host = np.zeros(nd)
     e2e = []
@@ -262,9 +278,11 @@ def main():
         "metric": METRIC, "value": round(ms, 3), "unit": "ms", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded mesh generator, see config)",
-        "config": {"workload": workload, "precision": "FP32 inner PCG (tol 1e-4 rel. residual) + FP64 refinement "
-                   "(outer tol 1e-12)", "target_rel_err": TARGET_ERR, "rel_err_fp32_refine": err_timed,
-                   "rel_err_fp64": e64, "l2": "flushed before every step (512 MB write)",
+        "config": {"workload": workload, "precision": (f"FP32 inner PCG (rel. residual {refine['tol']:g}) + FP64 "
+                   f"refinement (true rel. residual {refine['outer_tol']:g})"),
+                   "fp64_stop": f"recursive rel. residual {plain64['tol']:g}",
+                   "target_rel_err": TARGET_ERR, "rel_err_fp32_refine": err_timed,
+                   "rel_err_fp64": e64_timed, "l2": "flushed before every step (512 MB write)",
                    "parallelism": "replicas" if world > 1 else "single GPU", "semantics": "consistent"},
         "fp64_ms": round(ms64, 3), "speedup_vs_fp64": round(ms64 / ms, 3),
         "pcg_iterations": its, "outer_iterations": infos[-1]["outer_iterations"],

@@ -413,8 +413,15 @@ void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, co
   // launch shapes
   c->smem64 = (size_t)P.np_max * c->vw * 2 * sizeof(double);
   c->smem32 = (size_t)P.np_max * c->vw * 2 * sizeof(float);
-  auto set_smem = [&](const void *k, size_t bytes) {
-    CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(bytes, 1)));
+  // The limit is an attribute of the kernel function (shared by every context
+  // in the process), so it is raised once to the device maximum; each launch
+  // still requests only its own patch size.
+  int smem_optin = 0;
+  CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
+  if (c->smem64 + 8192 > (size_t)smem_optin)
+    throw Fail{CFEM_ERR_INVALID_ARGUMENT, "patch too large for shared memory: lower patch_elems"};
+  auto set_smem = [&](const void *k, size_t) {
+    CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin - 8192));
   };
   int occ = 1;
   if (c->dim == 3) {

@@ -221,12 +221,12 @@ class Oracle:
         lib().orc_matvec(self._h, np.ascontiguousarray(x, np.float64), y)
         return y
 
-    def pcg(self, f, tol=1e-12, rule=1, maxit=1000000):
+    def pcg(self, f, tol=1e-12, rule=1, maxit=1000000, allow_maxit=False):
         x = np.zeros(self.ndof, np.float64)
         it = C.c_int32(0)
         rc = lib().orc_pcg(self._h, np.ascontiguousarray(f, np.float64), x, float(tol), int(rule), int(maxit),
                            C.byref(it))
-        if rc not in (0,):
+        if rc not in ((0, -4) if allow_maxit else (0,)):
             raise RuntimeError(f"oracle pcg failed: {rc}")
         return x, it.value
 
