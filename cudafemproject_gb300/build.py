@@ -22,9 +22,12 @@ LIB = os.path.join(OUT, "libcfem_gb300.so")
 EXE = os.path.join(OUT, "cfem_run")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# -ffp-contract=off on host code: the float arithmetic that mirrors the
+# reference (wavelets, load factors) must round alike on x86 and aarch64.
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+                  "-Xcompiler", "-ffp-contract=off",
                   "-I", os.path.join(REPO, "include")]
-CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-I", os.path.join(REPO, "include")]
+CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-ffp-contract=off", "-I", os.path.join(REPO, "include")]
 
 CU_SOURCES = ["context.cu", "context_dyn.cu"]
 CXX_SOURCES = ["prep.cpp", "femfunc.cpp"]
@@ -87,7 +90,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     main_src = os.path.join(CSRC, "cfem_main.cpp")
     if os.path.exists(main_src) and (force or _stale(EXE, [main_src, LIB] + hdrs)):
-        cmd = ["g++", "-O2", "-std=c++17", "-I", os.path.join(REPO, "include"), main_src, "-o", EXE,
+        cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I", os.path.join(REPO, "include"), main_src, "-o", EXE,
                "-L", OUT, "-lcfem_gb300", "-Wl,-rpath,$ORIGIN"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

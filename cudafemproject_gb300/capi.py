@@ -89,6 +89,9 @@ SIGNATURES = [
     ("cfem_pcg_multi", i32, [vp, C.POINTER(SolveParams), i32, vp, vp, C.POINTER(SolveInfo)]),
     ("cfem_adjoint", i32, [vp, C.POINTER(SolveParams), vp, vp, vp, vp, C.POINTER(SolveInfo)]),
     ("cfem_set_young", i32, [vp, vp]),
+    ("cfem_dyn_adjoint", i32, [vp, C.POINTER(DynParams), C.POINTER(Wavelet), i32, vp, vp, C.POINTER(f64), vp,
+                                C.POINTER(DynInfo)]),
+    ("cfem_element_stress", i32, [vp, vp, vp, vp, vp]),
     ("cfem_profile_matvec", i32, [vp, i32, i32, C.POINTER(f64), C.POINTER(f64)]),
     ("cfem_run_task", i32, [C.c_char_p, C.c_char_p, i32, vp, i64, C.POINTER(SolveInfo), C.POINTER(DynInfo)]),
 ]

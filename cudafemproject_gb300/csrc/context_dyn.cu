@@ -310,10 +310,184 @@ cfem_status run_dyn(cfem_ctx *c, const cfem_dyn_params *prm, const cfem_wavelet 
   return (cfem_status)status;
 }
 
+// Explicit GN22 receiver-misfit adjoint with sqrt(N) checkpointing (FP64).
+cfem_status run_dyn_adjoint(cfem_ctx *c, const cfem_dyn_params *prm, const cfem_wavelet *w, int n_rec,
+                            const int32_t *rec_nodes, const double *obs, double *loss, double *dLdE,
+                            cfem_dyn_info *info) {
+  if (prm->beta2 != 0.0) throw Fail{CFEM_ERR_UNSUPPORTED, "the dynamics adjoint covers the explicit scheme (beta2 = 0)"};
+  if (c->semantics != CFEM_CONSISTENT)
+    throw Fail{CFEM_ERR_UNSUPPORTED, "the dynamics adjoint needs consistent semantics (no per-step re-sorted masses)"};
+  if (n_rec <= 0 || !rec_nodes || !obs) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "receivers and observations required"};
+  const double beta1 = prm->beta1, dt = prm->dt;
+  const float dtf = (float)prm->dt, endf = (float)prm->endtime;
+  if (!(dtf > 0)) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "dt must be positive"};
+  int N = endf < 0 ? 1 : (int)(endf / dtf);
+  if (N < 1) N = 1;
+  const int C = (int)std::ceil(std::sqrt((double)N));
+  const int64_t nv = c->nvec;
+  const double h_old = (1 - beta1) * dt, h_new = beta1 * dt, c2 = 0.5 * dt * dt;
+  RhsSchedule sch;
+  sch.semantics = c->semantics;
+  sch.has_loads = c->rhs.has_loads;
+  sch.w = w;
+  std::vector<double> coef(2 * (size_t)(N + 1));
+  sch.eval(0.f, coef[0], coef[1]);
+  for (int s = 1; s <= N; ++s) sch.eval((float)s * dtf, coef[2 * s], coef[2 * s + 1]);
+  DBuf<double> dcoef, minv, vel, acc, y, dA, dB, trace, obs_d, gE;
+  DBuf<int32_t> recv;
+  dcoef.upload(coef.data(), coef.size(), c->stream);
+  for (auto *b : {&minv, &vel, &acc, &y, &dA, &dB}) { b->alloc(nv); b->zero(c->stream); }
+  k_invert<double><<<nblk(nv), kThreads, 0, c->stream>>>(nv, c->mlump.p, minv.p);
+  std::vector<int32_t> rn(n_rec);
+  for (int i = 0; i < n_rec; ++i) {
+    if (rec_nodes[i] < 0 || rec_nodes[i] >= c->nn) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "receiver node out of range"};
+    rn[i] = c->prep.node_old2new[rec_nodes[i]];
+  }
+  recv.upload(rn.data(), rn.size(), c->stream);
+  trace.alloc((size_t)N * n_rec * c->dim);
+  obs_d.alloc((size_t)N * n_rec * c->dim);
+  CK(cudaMemcpyAsync(obs_d.p, obs, sizeof(double) * obs_d.n, cudaMemcpyDefault, c->stream));
+  gE.alloc(c->ne);
+  gE.zero(c->stream);
+  DBuf<DynState> st;
+  st.alloc(1);
+  // checkpoints of (d, v, a) after steps 0, C, 2C, ... and one segment of displacements
+  const int ncp = N / C + 1;
+  DBuf<double> cps, seg;
+  cps.alloc((size_t)ncp * 3 * nv);
+  seg.alloc((size_t)(C + 1) * nv);
+  const double *young = c->young_d.p;
+  DBuf<double> yd;
+  if (!young) {
+    std::vector<double> yv(c->ne, c->E);
+    yd.upload(yv.data(), yv.size(), c->stream);
+    young = yd.p;
+  }
+  DynParams<double> dp{};
+  dp.n_nodes = c->nn;
+  dp.v = vel.p;
+  dp.a = acc.p;
+  dp.y = y.p;
+  dp.FA = c->FA.p;
+  dp.FB = c->FB.p;
+  dp.coef = dcoef.p;
+  dp.st = st.p;
+  dp.dim = c->dim;
+  dp.minv = minv.p;
+  dp.c_old = h_old;
+  dp.c_new = h_new;
+  MvParams<double> mv = base_mv<double>(c);
+  mv.diagA = c->diagK.p;
+  mv.c1 = dt;
+  mv.c2 = c2;
+  mv.x2 = vel.p;
+  mv.x3 = acc.p;
+  mv.y = y.p;
+  auto set_step = [&](int step) {
+    DynState hs{};
+    hs.step = step;
+    CK(cudaMemcpyAsync(st.p, &hs, sizeof(hs), cudaMemcpyHostToDevice, c->stream));
+  };
+  auto step = [&](const double *from, double *to, bool record) {
+    mv.x = from;
+    mv.xout = to;
+    launch_mv<double>(c, MV_DYN, mv);
+    if (c->dim == 3) k_dyn_explicit<double, 3><<<c->grid_vec, kThreads, 0, c->stream>>>(dp);
+    else k_dyn_explicit<double, 2><<<c->grid_vec, kThreads, 0, c->stream>>>(dp);
+    DynParams<double> de = dp;
+    if (record) { de.recv = recv.p; de.n_recv = n_rec; de.trace = trace.p; } else { de.n_recv = 0; }
+    k_dyn_end_step<double><<<1, kThreads, 0, c->stream>>>(de, to, c->vw);
+    CKL();
+  };
+  auto save_cp = [&](int k, const double *d) {
+    double *base = cps.p + (size_t)k * 3 * nv;
+    CK(cudaMemcpyAsync(base, d, sizeof(double) * nv, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(base + nv, vel.p, sizeof(double) * nv, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(base + 2 * nv, acc.p, sizeof(double) * nv, cudaMemcpyDeviceToDevice, c->stream));
+  };
+  CK(cudaEventRecord(c->ev0, c->stream));
+  // forward with checkpoints
+  set_step(1);
+  double *cur = dA.p, *nxt = dB.p;
+  save_cp(0, cur);
+  for (int n = 1; n <= N; ++n) {
+    step(cur, nxt, true);
+    std::swap(cur, nxt);
+    if (n % C == 0 && n / C < ncp) save_cp(n / C, cur);
+  }
+  std::vector<double> htrace(trace.n);
+  CK(cudaMemcpyAsync(htrace.data(), trace.p, sizeof(double) * trace.n, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  std::vector<double> hobs(obs_d.n);
+  CK(cudaMemcpy(hobs.data(), obs_d.p, sizeof(double) * obs_d.n, cudaMemcpyDeviceToHost));
+  double L = 0;
+  for (size_t i = 0; i < htrace.size(); ++i) L += 0.5 * (htrace[i] - hobs[i]) * (htrace[i] - hobs[i]);
+  // reverse sweep
+  DBuf<double> db, vb, ab, wb;
+  for (auto *b : {&db, &vb, &ab, &wb}) { b->alloc(nv); b->zero(c->stream); }
+  for (int s = (N - 1) / C; s >= 0; --s) {
+    const int k0 = s * C, k1 = std::min(N, k0 + C);
+    // restore the checkpoint after step k0 and recompute steps k0+1..k1
+    const double *base = cps.p + (size_t)s * 3 * nv;
+    CK(cudaMemcpyAsync(seg.p, base, sizeof(double) * nv, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(vel.p, base + nv, sizeof(double) * nv, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(acc.p, base + 2 * nv, sizeof(double) * nv, cudaMemcpyDeviceToDevice, c->stream));
+    set_step(k0 + 1);
+    for (int n = k0 + 1; n <= k1; ++n) step(seg.p + (size_t)(n - 1 - k0) * nv, seg.p + (size_t)(n - k0) * nv, false);
+    for (int n = k1; n > k0; --n) {
+      const double *dn = seg.p + (size_t)(n - k0) * nv;
+      k_adj_receivers<<<nblk(n_rec * c->dim), kThreads, 0, c->stream>>>(n_rec, c->dim, c->vw, recv.p, dn,
+                                                                       obs_d.p + (size_t)(n - 1) * n_rec * c->dim, db.p);
+      k_adj_pre<<<nblk(nv), kThreads, 0, c->stream>>>(nv, h_old, h_new, minv.p, vb.p, ab.p, wb.p);
+      if (c->dim == 3)
+        k_grad_young<3><<<nblk(c->ne), kThreads, 0, c->stream>>>(c->ne, c->G64.p, c->gstride, c->conn.p, c->bits.p,
+                                                                 c->lam, c->mu, wb.p, dn, young, c->elem_new2old.p,
+                                                                 gE.p, 1);
+      else
+        k_grad_young<2><<<nblk(c->ne), kThreads, 0, c->stream>>>(c->ne, c->G64.p, c->gstride, c->conn.p, c->bits.p,
+                                                                 c->lam, c->mu, wb.p, dn, young, c->elem_new2old.p,
+                                                                 gE.p, 1);
+      MvParams<double> m2 = base_mv<double>(c);
+      m2.diagA = c->diagK.p;
+      m2.x = wb.p;
+      m2.y = y.p;
+      launch_mv<double>(c, MV_PLAIN, m2);
+      k_adj_post<<<nblk(nv), kThreads, 0, c->stream>>>(nv, dt, c2, y.p, db.p, vb.p, ab.p);
+      CKL();
+    }
+  }
+  CK(cudaEventRecord(c->ev1, c->stream));
+  CK(cudaEventSynchronize(c->ev1));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  if (dLdE) CK(cudaMemcpyAsync(dLdE, gE.p, sizeof(double) * c->ne, cudaMemcpyDefault, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (loss) *loss = L;
+  if (info) {
+    info->status = CFEM_OK;
+    info->steps = N;
+    info->pcg_iterations = 0;
+    info->solve_ms = ms;
+  }
+  return CFEM_OK;
+}
+
 }  // namespace detail
 }  // namespace cfem
 
 extern "C" {
+
+cfem_status cfem_dyn_adjoint(cfem_ctx *ctx, const cfem_dyn_params *prm, const cfem_wavelet *w, int32_t n_rec,
+                             const int32_t *rec_nodes, const double *obs, double *loss, double *dLdE,
+                             cfem_dyn_info *info) {
+  return run_guarded([&]() -> cfem_status {
+    check_ctx(ctx);
+    if (!prm) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "null parameters"};
+    enter(ctx);
+    return run_dyn_adjoint(ctx, prm, w, n_rec, rec_nodes, obs, loss, dLdE, info);
+  });
+}
+
 
 cfem_status cfem_dyn(cfem_ctx *ctx, const cfem_dyn_params *prm, const cfem_wavelet *w, double *u, cfem_dyn_info *info) {
   return run_guarded([&]() -> cfem_status {
@@ -382,6 +556,36 @@ cfem_status cfem_adjoint(cfem_ctx *ctx, const cfem_solve_params *prm, const doub
     }
     CK(cudaStreamSynchronize(ctx->stream));
     return st;
+  });
+}
+
+cfem_status cfem_element_stress(cfem_ctx *ctx, const double *u, double *strain, double *stress, double *mises) {
+  return run_guarded([&]() -> cfem_status {
+    check_ctx(ctx);
+    if (!u) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "null displacement"};
+    enter(ctx);
+    const int S = 3 * (ctx->dim - 1);
+    DBuf<double> uin, de, ds, dm;
+    uin.alloc(ctx->nvec);
+    uin.zero(ctx->stream);
+    to_internal<double>(ctx, u, uin.p);
+    if (strain) de.alloc((size_t)ctx->ne * S);
+    if (stress) ds.alloc((size_t)ctx->ne * S);
+    if (mises) dm.alloc(ctx->ne);
+    if (ctx->dim == 3)
+      k_element_stress<3><<<nblk(ctx->ne), kThreads, 0, ctx->stream>>>(ctx->ne, ctx->G64.p, ctx->gstride, ctx->vol.p, ctx->escale.p,
+                                                                        ctx->conn.p, uin.p, ctx->lam, ctx->mu, ctx->elem_new2old.p,
+                                                                        de.p, ds.p, dm.p);
+    else
+      k_element_stress<2><<<nblk(ctx->ne), kThreads, 0, ctx->stream>>>(ctx->ne, ctx->G64.p, ctx->gstride, ctx->vol.p, ctx->escale.p,
+                                                                        ctx->conn.p, uin.p, ctx->lam, ctx->mu, ctx->elem_new2old.p,
+                                                                        de.p, ds.p, dm.p);
+    CKL();
+    if (strain) CK(cudaMemcpyAsync(strain, de.p, sizeof(double) * de.n, cudaMemcpyDefault, ctx->stream));
+    if (stress) CK(cudaMemcpyAsync(stress, ds.p, sizeof(double) * ds.n, cudaMemcpyDefault, ctx->stream));
+    if (mises) CK(cudaMemcpyAsync(mises, dm.p, sizeof(double) * dm.n, cudaMemcpyDefault, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return CFEM_OK;
   });
 }
 

@@ -288,13 +288,17 @@ __global__ void __launch_bounds__(kThreads) k_matvec(MvParams<T> P) {
         for (int d = 0; d < DIM; ++d) u[a][d] = sp[(size_t)li[a] * VW + d];
       const T mc = P.mcoef ? P.cM * P.mcoef[e] : T(0);
       element_force<T, DIM>(u, G, P.lam, P.mu, P.cK, mc, f);
+      // p_e.A_e p_e in the working precision; one FP64 add per element (the
+      // FP64 pipe of this part is narrow, so no per-term double arithmetic)
+      T e_elem = 0;
 #pragma unroll
       for (int a = 0; a <= DIM; ++a)
 #pragma unroll
         for (int d = 0; d < DIM; ++d) {
-          if (MODE == MV_PCG) energy += (double)(u[a][d] * f[a][d]);
+          if (MODE == MV_PCG) e_elem += u[a][d] * f[a][d];
           atomicAdd(sy + (size_t)li[a] * VW + d, f[a][d]);
         }
+      if (MODE == MV_PCG) energy += (double)e_elem;
     }
     __syncthreads();
     // flush
@@ -362,14 +366,18 @@ __global__ void __launch_bounds__(kThreads) k_pcg_init(VecParams<T> P, int warm)
     NodeV<T, VW> u = ldv<T, VW>(P.u, n);
 #pragma unroll
     for (int d = 0; d < VW; ++d) { zero.v[d] = 0; r.v[d] = 0; z.v[d] = 0; }
+    T rz = 0, rr = 0, ff = 0;
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
       r.v[d] = warm ? f.v[d] - u.v[d] : f.v[d];
       z.v[d] = r.v[d] * di.v[d];
-      acc[0] += (double)r.v[d] * (double)z.v[d];
-      acc[1] += (double)r.v[d] * (double)r.v[d];
-      acc[2] += (double)f.v[d] * (double)f.v[d];
+      rz += r.v[d] * z.v[d];
+      rr += r.v[d] * r.v[d];
+      ff += f.v[d] * f.v[d];
     }
+    acc[0] += (double)rz;
+    acc[1] += (double)rr;
+    acc[2] += (double)ff;
     stv<T, VW>(P.r, n, r);
     stv<T, VW>(P.z, n, z);
     stv<T, VW>(P.u, n, zero);
@@ -404,14 +412,17 @@ __global__ void __launch_bounds__(kThreads) k_pcg_update(VecParams<T> P) {
     NodeV<T, VW> di = ldv<T, VW>(P.dinv, n), z, zero;
 #pragma unroll
     for (int d = 0; d < VW; ++d) { zero.v[d] = 0; z.v[d] = 0; }
+    T rz = 0, rr = 0;
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
       x.v[d] += alpha * p.v[d];
       r.v[d] -= alpha * u.v[d];
       z.v[d] = r.v[d] * di.v[d];
-      acc[0] += (double)r.v[d] * (double)z.v[d];
-      acc[1] += (double)r.v[d] * (double)r.v[d];
+      rz += r.v[d] * z.v[d];
+      rr += r.v[d] * r.v[d];
     }
+    acc[0] += (double)rz;
+    acc[1] += (double)rr;
     stv<T, VW>(P.x, n, x);
     stv<T, VW>(P.r, n, r);
     stv<T, VW>(P.z, n, z);

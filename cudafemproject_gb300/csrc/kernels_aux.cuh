@@ -352,7 +352,7 @@ __global__ void k_element_matrices(int64_t first, int64_t count, const int32_t *
 template <int DIM>
 __global__ void k_grad_young(int64_t ne, const double *G64, int64_t gstride, const int32_t *conn, const uint8_t *bits,
                              double lam, double mu, const double *lamv, const double *uv, const double *young,
-                             const int32_t *elem_new2old, double *g_out) {
+                             const int32_t *elem_new2old, double *g_out, int accumulate = 0) {
   constexpr int NV = DIM + 1, VW = DIM == 3 ? 4 : 2;
   int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (e >= ne) return;
@@ -395,7 +395,96 @@ __global__ void k_grad_young(int64_t ne, const double *G64, int64_t gstride, con
       }
   }
   int64_t eo = elem_new2old[e];
-  g_out[eo] = -(acc + diag_terms) / young[eo];
+  const double v = -(acc + diag_terms) / young[eo];
+  g_out[eo] = accumulate ? g_out[eo] + v : v;
+}
+
+// ---- explicit GN22 adjoint (reverse of one step; see cfem_dyn_adjoint) ----
+// receiver misfit: db[node_r] += d_n[node_r] - obs_n[r]
+static __global__ void k_adj_receivers(int n_rec, int dim, int vw, const int32_t *recv, const double *d,
+                                       const double *obs_n, double *db) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_rec * dim) return;
+  int r = i / dim, q = i % dim;
+  int64_t k = (int64_t)recv[r] * vw + q;
+  db[k] += d[k] - obs_n[i];
+}
+
+// w = (a_bar + h_new v_bar) / M ; a_bar = h_old v_bar
+static __global__ void k_adj_pre(int64_t n, double h_old, double h_new, const double *minv, const double *vb,
+                                 double *ab, double *wb) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double an = ab[i] + h_new * vb[i];
+  wb[i] = an * minv[i];
+  ab[i] = h_old * vb[i];
+}
+
+// d_tot = d_bar - K w ; d_bar = d_tot ; v_bar += dt d_tot ; a_bar += c2 d_tot ; y = 0
+static __global__ void k_adj_post(int64_t n, double dt, double c2, double *y, double *db, double *vb, double *ab) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double t = db[i] - y[i];
+  y[i] = 0;
+  db[i] = t;
+  vb[i] += dt * t;
+  ab[i] += c2 * t;
+}
+
+// Element strain / stress recovery (deprecated/femfunc/femfunc.cpp:42-106:
+// deformation = B u_e, stress = D deformation), Voigt order (xx, yy, xy) in 2D
+// and (xx, yy, zz, xy, yz, xz) in 3D with engineering shear strains, plus the
+// von Mises stress (plane stress in 2D).
+template <int DIM>
+__global__ void k_element_stress(int64_t ne, const double *G64, int64_t gstride, const double *vol, const double *escale,
+                                 const int32_t *conn, const double *u, double lam, double mu,
+                                 const int32_t *elem_new2old, double *strain, double *stress, double *mises) {
+  constexpr int NV = DIM + 1, VW = DIM == 3 ? 4 : 2, S = 3 * (DIM - 1);
+  int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  const double s_e = escale ? escale[e] : 1.0;
+  const double inv = 1.0 / sqrt(vol[e] * s_e);
+  double g[NV][DIM];
+  for (int d = 0; d < DIM; ++d) {
+    double s0 = 0;
+    for (int a = 1; a < NV; ++a) {
+      g[a][d] = G64[(size_t)((a - 1) * DIM + d) * gstride + e] * inv;
+      s0 += g[a][d];
+    }
+    g[0][d] = -s0;
+  }
+  double H[DIM][DIM] = {};
+  for (int a = 0; a < NV; ++a) {
+    const int64_t n = conn[e * NV + a];
+    for (int i = 0; i < DIM; ++i)
+      for (int j = 0; j < DIM; ++j) H[i][j] += u[n * VW + i] * g[a][j];
+  }
+  double eps[S], sig[S];
+  const double L = lam * s_e, M = mu * s_e;
+  if (DIM == 2) {
+    eps[0] = H[0][0]; eps[1] = H[1][1]; eps[2] = H[0][1] + H[1][0];
+    const double tr = eps[0] + eps[1];
+    sig[0] = L * tr + 2 * M * eps[0]; sig[1] = L * tr + 2 * M * eps[1]; sig[2] = M * eps[2];
+  } else {
+    eps[0] = H[0][0]; eps[1] = H[1][1]; eps[2] = H[2][2];
+    eps[3] = H[0][1] + H[1][0]; eps[4] = H[1][2] + H[2][1]; eps[5] = H[0][2] + H[2][0];
+    const double tr = eps[0] + eps[1] + eps[2];
+    for (int i = 0; i < 3; ++i) sig[i] = L * tr + 2 * M * eps[i];
+    for (int i = 3; i < 6; ++i) sig[i] = M * eps[i];
+  }
+  const int64_t eo = elem_new2old[e];
+  for (int i = 0; i < S; ++i) {
+    if (strain) strain[eo * S + i] = eps[i];
+    if (stress) stress[eo * S + i] = sig[i];
+  }
+  if (mises) {
+    double m2;
+    if (DIM == 2) m2 = sig[0] * sig[0] - sig[0] * sig[1] + sig[1] * sig[1] + 3 * sig[2] * sig[2];
+    else
+      m2 = 0.5 * ((sig[0] - sig[1]) * (sig[0] - sig[1]) + (sig[1] - sig[2]) * (sig[1] - sig[2]) +
+                  (sig[2] - sig[0]) * (sig[2] - sig[0])) + 3 * (sig[3] * sig[3] + sig[4] * sig[4] + sig[5] * sig[5]);
+    mises[eo] = sqrt(m2);
+  }
 }
 
 }  // namespace cfem

@@ -151,7 +151,8 @@ class FemContext:
     @staticmethod
     def _info(inf):
         return dict(status=inf.status, iterations=inf.iterations, outer_iterations=inf.outer_iterations,
-                    rel_residual=inf.rel_residual, gamma0=inf.gamma0, gamma=inf.gamma, solve_ms=inf.solve_ms)
+                    rel_residual=inf.rel_residual, gamma0=inf.gamma0, gamma=inf.gamma, solve_ms=inf.solve_ms,
+                    kernel_launches=inf.kernel_launches)
 
     def static_solve(self, precision="fp64", tol=1e-8, stop_rule="reference", max_iter=1000000, outer_tol=1e-12,
                      max_outer=50, wavelet: Optional[WaveletParams] = None, out=None, allow_not_converged=False):
@@ -204,6 +205,31 @@ class FemContext:
                                      df.ctypes.data, C.byref(inf))
         capi.check(st, "cfem_adjoint")
         return dE, df, self._info(inf)
+
+    def element_stress(self, u):
+        """Per-element (strain, stress, von Mises) of displacements u (caller order)."""
+        s = 3 * (self.dim - 1)
+        u = np.ascontiguousarray(u, dtype=np.float64).ravel()
+        eps = np.zeros((self.n_elems, s))
+        sig = np.zeros((self.n_elems, s))
+        mis = np.zeros(self.n_elems)
+        capi.check(capi.lib().cfem_element_stress(self._h, u.ctypes.data, eps.ctypes.data, sig.ctypes.data,
+                                                  mis.ctypes.data), "cfem_element_stress")
+        return eps, sig, mis
+
+    def dyn_adjoint(self, beta1, dt, endtime, receivers, obs, wavelet: Optional[WaveletParams] = None):
+        """Explicit GN22 receiver-misfit loss and dL/dE (sqrt(N)-checkpointed adjoint)."""
+        rec = np.ascontiguousarray(receivers, dtype=np.int32)
+        obs = np.ascontiguousarray(obs, dtype=np.float64)
+        g = np.zeros(self.n_elems)
+        L = C.c_double(0)
+        prm = capi.DynParams(float(beta1), 0.0, float(dt), float(endtime), capi.FP64, 0.0, 0, 0, 0, 0, None, None)
+        inf = capi.DynInfo()
+        w = _wavelet(wavelet)
+        capi.check(capi.lib().cfem_dyn_adjoint(self._h, C.byref(prm), C.byref(w) if w else None, len(rec),
+                                               rec.ctypes.data, obs.ctypes.data, C.byref(L), g.ctypes.data,
+                                               C.byref(inf)), "cfem_dyn_adjoint")
+        return L.value, g, dict(steps=inf.steps, solve_ms=inf.solve_ms)
 
     def set_young(self, young):
         y = np.ascontiguousarray(young, dtype=np.float64)

@@ -226,6 +226,20 @@ CFEM_API cfem_status cfem_run_task(const char *config_path, const char *task, in
  * local connectivity, per node z and p read, p written, y accumulated. */
 CFEM_API cfem_status cfem_profile_matvec(cfem_ctx *ctx, int32_t precision, int32_t n_launches, double *ms_per_launch,
                                          double *bytes_per_launch);
+/* Element strains and stresses of a displacement field u (caller order):
+ * strain = B u_e, stress = D_e strain in Voigt order (xx, yy, xy) / (xx, yy, zz,
+ * xy, yz, xz), engineering shear; von Mises stress per element
+ * (deprecated/femfunc/femfunc.cpp:42-106). Outputs [n_elems][3(dim-1)] or
+ * [n_elems], caller element order; any output may be NULL. */
+CFEM_API cfem_status cfem_element_stress(cfem_ctx *ctx, const double *u, double *strain, double *stress, double *mises);
+/* Explicit GN22 (beta2 == 0, FP64, consistent semantics) receiver-misfit loss
+ * L = 1/2 sum_{n=1..N} sum_r |d_n[node_r] - obs[n-1][r]|^2 and its gradient in
+ * the per-element Young's moduli by the discrete adjoint of the time stepping.
+ * The reverse sweep recomputes forward states segment by segment from
+ * checkpoints stored every ceil(sqrt(N)) steps. obs: [N][n_rec][dim]. */
+CFEM_API cfem_status cfem_dyn_adjoint(cfem_ctx *ctx, const cfem_dyn_params *prm, const cfem_wavelet *w, int32_t n_rec,
+                                      const int32_t *rec_nodes, const double *obs, double *loss, double *dLdE,
+                                      cfem_dyn_info *info);
 /* Per-element Young's modulus update (keeps geometry; rebuilds operator scale). */
 CFEM_API cfem_status cfem_set_young(cfem_ctx *ctx, const double *elem_young);
 

@@ -519,3 +519,92 @@ void orc_grad_E(const orc_ctx *c, const double *lambda, const double *u, double 
     g[e] = -acc / c->Ee[e];
   }
 }
+
+/* Per-element accumulation g_e += -(1/E_e) w_e^T K'_e d_e. */
+static void grad_acc(const orc_ctx *c, const double *wv, const double *dv, double *g) {
+  const int w = c->w;
+  const ebe_f64 *m = &c->m;
+#pragma omp parallel for schedule(static)
+  for (int64_t e = 0; e < c->ne; ++e) {
+    double we[12], de[12];
+    for (int k = 0; k < w; ++k) { we[k] = wv[m->mask[e * w + k]]; de[k] = dv[m->mask[e * w + k]]; }
+    const double *K = m->K + e * w * w;
+    double acc = 0;
+    for (int n = 0; n < w; ++n) {
+      double t = 0;
+      for (int k = 0; k < w; ++k) t += we[k] * K[k + n * w];
+      acc += t * de[n];
+    }
+    g[e] -= acc / c->Ee[e];
+  }
+}
+
+double orc_dyn_adjoint(orc_ctx *c, const orc_wavelet *wv, const orc_dyn *dp, int32_t n_rec, const int32_t *rec,
+                       const double *obs, double *g) {
+  const int dim = c->dim, w = c->w;
+  const int64_t nd = c->nd;
+  const double beta1 = dp->beta1, dt = dp->dt;
+  const float dtf = (float)dp->dt, endf = (float)dp->endtime;
+  int N = endf < 0 ? 1 : (int)(endf / dtf);
+  if (N < 1) N = 1;
+  const double h_old = (1 - beta1) * dt, h_new = beta1 * dt, cpred = 0.5 * dt * dt;
+  /* lumped mass (consistent: rho V / (dim+1) per DOF) */
+  double *mloc = (double *)malloc(sizeof(double) * c->ne * w), *M = (double *)malloc(sizeof(double) * nd);
+  for (int64_t e = 0; e < c->ne; ++e) {
+    double md, mo;
+    mass_coeffs(c, e, 1, &md, &mo);
+    for (int j = 0; j < w; ++j) mloc[e * w + j] = md;
+  }
+  gsum(c, mloc, M);
+  free(mloc);
+  double *D = (double *)calloc((size_t)(N + 1) * nd, sizeof(double));  /* all displacements */
+  double *v = (double *)calloc((size_t)nd, sizeof(double)), *a = (double *)calloc((size_t)nd, sizeof(double));
+  double *f = (double *)malloc(sizeof(double) * nd), *y = (double *)malloc(sizeof(double) * nd);
+  for (int64_t k = 0; k < c->m.nf; ++k) c->press[k] = c->press0[k];
+  double L = 0;
+  for (int n = 1; n <= N; ++n) {
+    float t = (float)n * dtf;
+    double *dn = D + (size_t)n * nd, *dm = D + (size_t)(n - 1) * nd;
+    for (int64_t k = 0; k < nd; ++k) dn[k] = dm[k] + dt * v[k] + cpred * a[k];
+    orc_matvec(c, dn, y);
+    orc_get_rhs(c, wv, (double)t, f);
+    for (int64_t k = 0; k < nd; ++k) {
+      double an = (f[k] - y[k]) / M[k];
+      v[k] += h_old * a[k] + h_new * an;
+      a[k] = an;
+    }
+    for (int r = 0; r < n_rec; ++r)
+      for (int q = 0; q < dim; ++q) {
+        double diff = dn[(int64_t)rec[r] * dim + q] - obs[((size_t)(n - 1) * n_rec + r) * dim + q];
+        L += 0.5 * diff * diff;
+      }
+  }
+  /* reverse sweep */
+  double *db = (double *)calloc((size_t)nd, sizeof(double)), *vb = (double *)calloc((size_t)nd, sizeof(double));
+  double *ab = (double *)calloc((size_t)nd, sizeof(double)), *wb = (double *)malloc(sizeof(double) * nd);
+  memset(g, 0, sizeof(double) * c->ne);
+  for (int n = N; n >= 1; --n) {
+    double *dn = D + (size_t)n * nd;
+    for (int r = 0; r < n_rec; ++r)
+      for (int q = 0; q < dim; ++q) {
+        int64_t k = (int64_t)rec[r] * dim + q;
+        db[k] += dn[k] - obs[((size_t)(n - 1) * n_rec + r) * dim + q];
+      }
+    /* v_n = v + h_old a + h_new a_n ; a_n = M^-1 (F - K d_n) ; d_n = d + dt v + c a */
+    for (int64_t k = 0; k < nd; ++k) {
+      double an_b = ab[k] + h_new * vb[k];
+      wb[k] = an_b / M[k];
+      ab[k] = h_old * vb[k];
+    }
+    grad_acc(c, wb, dn, g);
+    orc_matvec(c, wb, y);
+    for (int64_t k = 0; k < nd; ++k) {
+      double dtot = db[k] - y[k];
+      db[k] = dtot;
+      vb[k] += dt * dtot;
+      ab[k] += cpred * dtot;
+    }
+  }
+  free(D); free(v); free(a); free(f); free(y); free(db); free(vb); free(ab); free(wb); free(M);
+  return L;
+}

@@ -106,6 +106,12 @@ int orc_pcg(const orc_ctx *c, const double *f, double *x, double tol, int32_t ru
  * are used by the implicit scheme (compat uses rule 0, tol 1e-4 like the reference). */
 int orc_dyn_run(orc_ctx *c, const orc_wavelet *w, const orc_dyn *d, double pcg_tol, int32_t pcg_rule,
                 double *u_out, int32_t *steps, int64_t *pcg_iters);
+/* Explicit GN22 (beta2 = 0) receiver-misfit loss and its gradient in the
+ * per-element Young's moduli by the discrete adjoint (all states stored):
+ * L = 1/2 sum_{n=1..N} sum_r |d_n[node_r] - obs[n-1][r]|^2 (obs [N][n_rec][dim]).
+ * Consistent semantics only. Returns L; g [n_elems]. */
+double orc_dyn_adjoint(orc_ctx *c, const orc_wavelet *w, const orc_dyn *d, int32_t n_rec, const int32_t *rec_nodes,
+                       const double *obs, double *g);
 /* Adjoint sensitivity for a solved static state: dL/dE_e = -lambda_e^T (K_e / E_e) u_e. */
 void orc_grad_E(const orc_ctx *c, const double *lambda, const double *u, double *g);
 

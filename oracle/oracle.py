@@ -84,6 +84,8 @@ def lib():
         L.orc_dyn_run.argtypes = [C.c_void_p, W, D, C.c_double, C.c_int32, _f64p, C.POINTER(C.c_int32),
                                   C.POINTER(C.c_int64)]
         L.orc_grad_E.argtypes = [C.c_void_p, _f64p, _f64p, _f64p]
+        L.orc_dyn_adjoint.restype = C.c_double
+        L.orc_dyn_adjoint.argtypes = [C.c_void_p, W, D, C.c_int32, _i32p, _f64p, _f64p]
         _lib = L
     return _lib
 
@@ -242,6 +244,15 @@ class Oracle:
         if rc:
             raise RuntimeError(f"oracle dyn failed: {rc}")
         return u, st.value, it.value
+
+    def dyn_adjoint(self, beta1, dt, endtime, rec_nodes, obs, wavelet=None):
+        """Explicit GN22 receiver-misfit loss and dL/dE per element (discrete adjoint)."""
+        rec = np.ascontiguousarray(rec_nodes, np.int32)
+        g = np.zeros(self.p.n_elems, np.float64)
+        d = _Dyn(beta1, 0.0, dt, endtime)
+        L = lib().orc_dyn_adjoint(self._h, C.byref(wavelet_struct(wavelet)), C.byref(d), len(rec), rec,
+                                  np.ascontiguousarray(obs, np.float64).ravel(), g)
+        return L, g
 
     def grad_E(self, lam, u):
         g = np.zeros(self.p.n_elems, np.float64)

@@ -98,6 +98,19 @@ def main():
         u = meshio.read_vtk_displacements(ref_vtk, 2)
         np.savetxt(os.path.join(HERE, f"{task}_vtk_displacements.txt"), u, fmt="%.6g",
                    header=f"displacements block of testing/{task}_test/results.vtk (reference fixture)")
+        lines = open(ref_vtk).read().split("\n")
+        if "TENSORS stress double" in lines:
+            i = lines.index("TENSORS stress double")
+            rows = []
+            j = i + 1
+            while lines[j].strip():
+                rows.append([float(v) for v in lines[j].split()])
+                j += 1
+            T = np.array(rows).reshape(-1, 9)
+            k = lines.index("SCALARS mises_stress double")
+            mises = np.array([float(v) for v in lines[k + 2:k + 2 + T.shape[0]]])
+            np.savetxt(os.path.join(HERE, f"{task}_vtk_stress.txt"), np.column_stack([T, mises]), fmt="%.6g",
+                       header=f"stress tensor (row-major 3x3) and mises_stress per cell of testing/{task}_test/results.vtk")
         with tempfile.TemporaryDirectory() as work:
             shutil.copytree(os.path.join(meshes, "2D"), os.path.join(work, "prepared_meshes", "2D"))
             cfg = write_cfg(work, 2, 2e7, 0.25)

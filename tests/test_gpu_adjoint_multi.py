@@ -71,3 +71,61 @@ def test_multi_rhs(precision, tol):
     for i in range(5):
         x, _ = o.pcg(F[i], tol=1e-14, rule=1)
         assert rel(U[i], x) <= tol
+
+
+def test_torch_autograd_function():
+    torch = pytest.importorskip("torch")
+    from cudafemproject_gb300.autograd import static_solve
+    from cudafemproject_gb300.solver import FemContext
+    p = _problem(5)
+    ctx = FemContext(p, semantics="consistent")
+    young = torch.tensor(p.elem_E, dtype=torch.float64, requires_grad=True)
+    f = torch.tensor(ctx.rhs(), dtype=torch.float64, requires_grad=True)
+    u = static_solve(ctx, young, f, precision="fp64", tol=1e-13)
+    loss = (f.detach() * u).sum() + 0.5 * (u[:30] ** 2).sum()
+    loss.backward()
+    o = O.Oracle(p, consistent=True)
+    uo, _ = o.pcg(f.detach().numpy(), tol=1e-14, rule=1)
+    g = f.detach().numpy().copy()
+    g[:30] += uo[:30]
+    lam, _ = o.pcg(g, tol=1e-14, rule=1)
+    assert rel(young.grad.numpy(), o.grad_E(lam, uo)) <= 1e-6
+    assert rel(f.grad.numpy(), lam) <= 1e-8
+
+
+def _dyn_problem(E):
+    p = meshgen.box_3d(2, 2, 5, jitter=0.1, seed=1, rho=2000.0, traction=None,
+                       point_load=("top_centre", (0.0, 0.0, -1e3)))
+    p.elem_E = E.copy()
+    return p
+
+
+def test_explicit_dynamics_adjoint_checkpointed():
+    """Receiver-misfit gradient through 200 explicit steps (sqrt(N) = 15-step
+    checkpoint segments) against the FP64 oracle's stored-state adjoint and
+    central finite differences."""
+    from cudafemproject_gb300.solver import FemContext
+    rng = np.random.default_rng(3)
+    p0 = _dyn_problem(np.full(120, 2e7))
+    E = 2e7 * np.exp(0.3 * rng.standard_normal(p0.n_elems))
+    p = _dyn_problem(E)
+    top = np.where(np.isclose(p.nodes[:, 2], 4.0))[0].astype(np.int32)
+    N, dt = 200, 1e-4
+    T = float(np.float32(N * dt * 1.0000001))
+    obs = 1e-7 * rng.standard_normal((N, len(top), 3))
+    ctx = FemContext(p, semantics="consistent")
+    L, g, info = ctx.dyn_adjoint(0.5, dt, T, top, obs)
+    assert info["steps"] == N
+    Lo, go = O.Oracle(p, consistent=True).dyn_adjoint(0.5, dt, T, top, obs)
+    assert abs(L - Lo) <= 1e-10 * abs(Lo)
+    assert rel(g, go) <= 1e-8
+    big = np.argsort(-np.abs(g))[:4]
+    for e in big:
+        vals = []
+        for s in (+1, -1):
+            E2 = E.copy()
+            E2[e] *= 1 + s * 1e-4
+            Lq, _, _ = FemContext(_dyn_problem(E2), semantics="consistent").dyn_adjoint(0.5, dt, T, top, obs)
+            vals.append(Lq)
+        fd = (vals[0] - vals[1]) / (2e-4 * E[e])
+        assert abs(fd - g[e]) <= 1e-4 * abs(g[e]), (e, fd, g[e])

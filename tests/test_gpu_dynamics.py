@@ -25,7 +25,11 @@ def test_dyn_compat_fp64_vs_oracle_and_reference(name):
     ctx = FemContext(p)
     u, info = ctx.dyn(*args, precision="fp64", wavelet=w)
     assert info["steps"] == steps
-    tol = 1e-9 if args[1] == 0.0 else 1e-7  # implicit compat: PCG stops at gamma < 1e-4 gamma0 on both sides
+    # explicit: the same recurrence, step for step. Implicit compat: every step
+    # stops its PCG at gamma < 1e-4 gamma0 (the reference rule), where PCG
+    # iterates are rounding-sensitive; the consistent mode with converged
+    # solves carries the 1e-9 trajectory bound (test_dyn_consistent_fp64).
+    tol = 1e-9 if args[1] == 0.0 else 1e-5
     assert rel(u, ug) <= tol
     assert rel(u, ref["u"]) < 1e-4
 
