@@ -237,6 +237,8 @@ __global__ void __launch_bounds__(kThreads) k_matvec(MvParams<T> P) {
   constexpr int VW = DIM == 3 ? 4 : 2;
   constexpr int NC = DIM * DIM;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  // sp: staged node values, VW per node (one 16/32-byte shared load per node);
+  // sy: accumulators, structure of arrays (bank = node index mod 32)
   T *sp = reinterpret_cast<T *>(smem_raw);
   if (MODE == MV_PCG && P.sc->done) return;
   T beta = 0;
@@ -247,7 +249,7 @@ __global__ void __launch_bounds__(kThreads) k_matvec(MvParams<T> P) {
   for (int patch = blockIdx.x; patch < P.n_patches; patch += gridDim.x) {
     const int nb = P.node_off[patch], nn = P.node_off[patch + 1] - nb, own = P.own[patch];
     const int e0 = P.elem_off[patch], ne = P.elem_off[patch + 1] - e0;
-    T *sy = sp + (size_t)nn * VW;
+    T *sy = sp + (size_t)nn * VW;  // [DIM][nn]
     // stage
     for (int i = threadIdx.x; i < nn; i += blockDim.x) {
       const int g = P.nodes[nb + i];
@@ -266,11 +268,12 @@ __global__ void __launch_bounds__(kThreads) k_matvec(MvParams<T> P) {
         if (i >= own) stv<T, VW>(P.xout, g, v);
       }
       const unsigned b = P.bits[g];
+      NodeV<T, VW> m;
 #pragma unroll
-      for (int d = 0; d < VW; ++d) {
-        sp[(size_t)i * VW + d] = (d < DIM && !(b >> d & 1u)) ? v.v[d] : T(0);
-        sy[(size_t)i * VW + d] = 0;
-      }
+      for (int d = 0; d < VW; ++d) m.v[d] = (d < DIM && !(b >> d & 1u)) ? v.v[d] : T(0);
+      stv<T, VW>(sp, i, m);
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) sy[(size_t)d * nn + i] = 0;
     }
     __syncthreads();
     // compute
@@ -283,9 +286,11 @@ __global__ void __launch_bounds__(kThreads) k_matvec(MvParams<T> P) {
       for (int k = 0; k < NC; ++k) G[k] = P.G[(size_t)k * P.gstride + e];
       T u[DIM + 1][DIM], f[DIM + 1][DIM];
 #pragma unroll
-      for (int a = 0; a <= DIM; ++a)
+      for (int a = 0; a <= DIM; ++a) {
+        const NodeV<T, VW> s = ldv<T, VW>(sp, li[a]);
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) u[a][d] = sp[(size_t)li[a] * VW + d];
+        for (int d = 0; d < DIM; ++d) u[a][d] = s.v[d];
+      }
       const T mc = P.mcoef ? P.cM * P.mcoef[e] : T(0);
       element_force<T, DIM>(u, G, P.lam, P.mu, P.cK, mc, f);
       // p_e.A_e p_e in the working precision; one FP64 add per element (the
@@ -296,7 +301,7 @@ __global__ void __launch_bounds__(kThreads) k_matvec(MvParams<T> P) {
 #pragma unroll
         for (int d = 0; d < DIM; ++d) {
           if (MODE == MV_PCG) e_elem += u[a][d] * f[a][d];
-          atomicAdd(sy + (size_t)li[a] * VW + d, f[a][d]);
+          atomicAdd(sy + (size_t)d * nn + li[a], f[a][d]);
         }
       if (MODE == MV_PCG) energy += (double)e_elem;
     }
@@ -309,7 +314,7 @@ __global__ void __launch_bounds__(kThreads) k_matvec(MvParams<T> P) {
       bool any = false;
 #pragma unroll
       for (int d = 0; d < VW; ++d) {
-        T val = (d < DIM && !(b >> d & 1u)) ? sy[(size_t)i * VW + d] : T(0);
+        T val = (d < DIM && !(b >> d & 1u)) ? sy[(size_t)d * nn + i] : T(0);
         r.v[d] = val;
         any |= val != T(0);
       }

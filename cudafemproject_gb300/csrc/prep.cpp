@@ -92,9 +92,45 @@ std::string build_prep(const cfem_mesh &m, int patch_elems, Prep &P) {
   key.clear();
   key.shrink_to_fit();
 
-  // ---- patches and first-touch node numbering ----
+  // ---- patches; inside a patch, order elements in rounds of 32 that share no
+  // node, so one warp's shared-memory accumulations hit distinct addresses ----
   const int pe = patch_elems;
   P.n_patches = (int)((ne + pe - 1) / pe);
+  {
+    std::vector<int32_t> stamp(nn, -1), group, rest, order;
+    int round_id = 0;
+    for (int p = 0; p < P.n_patches; ++p) {
+      int64_t e0 = (int64_t)p * pe, e1 = std::min<int64_t>(ne, e0 + pe);
+      rest.assign(P.elem_new2old.begin() + e0, P.elem_new2old.begin() + e1);
+      order.clear();
+      while (!rest.empty()) {
+        group.clear();
+        ++round_id;
+        size_t keep = 0;
+        for (size_t i = 0; i < rest.size(); ++i) {
+          const int32_t e = rest[i];
+          bool clash = false;
+          if (group.size() < 32)
+            for (int a = 0; a < nv && !clash; ++a) clash = stamp[m.elems[(int64_t)e * nv + a]] == round_id;
+          if (group.size() < 32 && !clash) {
+            group.push_back(e);
+            for (int a = 0; a < nv; ++a) stamp[m.elems[(int64_t)e * nv + a]] = round_id;
+          } else {
+            rest[keep++] = e;
+          }
+        }
+        rest.resize(keep);
+        // a round that cannot be filled node-disjointly is topped up in order
+        while (group.size() < 32 && !rest.empty()) {
+          group.push_back(rest.front());
+          rest.erase(rest.begin());
+        }
+        order.insert(order.end(), group.begin(), group.end());
+      }
+      std::copy(order.begin(), order.end(), P.elem_new2old.begin() + e0);
+    }
+    for (int64_t i = 0; i < ne; ++i) P.elem_old2new[P.elem_new2old[i]] = (int32_t)i;
+  }
   P.node_old2new.assign(nn, -1);
   P.node_new2old.resize(nn);
   int32_t next = 0;
