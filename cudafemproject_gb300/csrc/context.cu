@@ -4,6 +4,8 @@
 // PCG iterations are issued as captured CUDA graphs of 2*chunk kernels
 // (matvec with fused direction update, then the vector update), replayed until
 // the device-side stopping flag is set; all scalar recurrences stay on the GPU.
+#include <mutex>
+
 #include "context_internal.cuh"
 #include "kernels_aux.cuh"
 
@@ -877,3 +879,156 @@ cfem_status cfem_profile_matvec(cfem_ctx *ctx, int32_t precision, int32_t n_laun
 }  // extern "C"
 
 // dynamics, multi-RHS and adjoint entry points live in context_dyn.cu
+
+// ============================================================ no-allocation matvec
+// cfem_matvec_energy_noalloc: y = K' x and e = x.K'x for callers that cannot
+// allocate device memory (see include/cfem.h). Its only scratch is this fixed
+// array: the per-block partial sums of e, the ticket counter of the last-block
+// reduction and the result slot. It is allocated when the library is loaded
+// and is held by every GPU that loads the library until the process exits.
+namespace cfem {
+namespace detail {
+
+constexpr int kNoAllocMaxBlocks = 4096;  // CFEM_NOALLOC_MAX_BLOCKS in include/cfem.h
+constexpr int kNoAllocCounter = kNoAllocMaxBlocks;      // slot holding the ticket counter
+constexpr int kNoAllocResult = kNoAllocMaxBlocks + 1;   // slot holding x.K'x
+constexpr int kNoAllocDoubles = kNoAllocMaxBlocks + 32;  // 32.9 KB in total
+
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocDoubles];
+
+// The PLAIN matvec reading x and accumulating y directly in the caller's node
+// order (no staging copies), with x.K'x reduced through the scratch array.
+template <int DIM>
+__global__ void __launch_bounds__(kThreads) k_matvec_noalloc(MvParams<double> P, const double *xc, double *yc,
+                                                             const int32_t *new2old, double *scratch) {
+  constexpr int VW = DIM == 3 ? 4 : 2;
+  constexpr int NC = DIM * DIM;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double *sp = reinterpret_cast<double *>(smem_raw);
+  double energy = 0;
+  for (int patch = blockIdx.x; patch < P.n_patches; patch += gridDim.x) {
+    const int nb = P.node_off[patch], nn = P.node_off[patch + 1] - nb, own = P.own[patch];
+    const int e0 = P.elem_off[patch], ne = P.elem_off[patch + 1] - e0;
+    double *sy = sp + (size_t)nn * VW;
+    for (int i = threadIdx.x; i < nn; i += blockDim.x) {
+      const int g = P.nodes[nb + i];
+      const int64_t o = new2old[g];
+      const unsigned b = P.bits[g];
+      for (int d = 0; d < VW; ++d) sp[(size_t)i * VW + d] = (d < DIM && !(b >> d & 1u)) ? xc[o * DIM + d] : 0.0;
+      for (int d = 0; d < DIM; ++d) sy[(size_t)d * nn + i] = 0;
+    }
+    __syncthreads();
+    for (int le = threadIdx.x; le < ne; le += blockDim.x) {
+      const int e = e0 + le;
+      const uint2 c = P.lconn[e];
+      const int li[4] = {(int)(c.x & 0xffffu), (int)(c.x >> 16), (int)(c.y & 0xffffu), (int)(c.y >> 16)};
+      double G[NC];
+      for (int k = 0; k < NC; ++k) G[k] = P.G[(size_t)k * P.gstride + e];
+      double u[DIM + 1][DIM], f[DIM + 1][DIM];
+      for (int a = 0; a <= DIM; ++a)
+        for (int d = 0; d < DIM; ++d) u[a][d] = sp[(size_t)li[a] * VW + d];
+      element_force<double, DIM>(u, G, P.lam, P.mu, 1.0, 0.0, f);
+      for (int a = 0; a <= DIM; ++a)
+        for (int d = 0; d < DIM; ++d) {
+          energy += u[a][d] * f[a][d];
+          atomicAdd(sy + (size_t)d * nn + li[a], f[a][d]);
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nn; i += blockDim.x) {
+      const int g = P.nodes[nb + i];
+      const int64_t o = new2old[g];
+      const unsigned b = P.bits[g];
+      for (int d = 0; d < DIM; ++d) {
+        double val = (b >> d & 1u) ? 0.0 : sy[(size_t)d * nn + i];
+        if ((b >> d & 1u) && i >= own) {  // (I - P) diag(K) x on constrained DOFs
+          const double xv = xc[o * DIM + d];
+          val = P.diagA[(int64_t)g * VW + d] * xv;
+          energy += val * xv;
+        }
+        if (val != 0.0) atomicAdd(yc + o * DIM + d, val);
+      }
+    }
+    __syncthreads();
+  }
+  double v[1] = {energy};
+  if (grid_sum_last<1>(v, scratch, reinterpret_cast<unsigned int *>(scratch + kNoAllocCounter)))
+    scratch[kNoAllocResult] = v[0];
+}
+
+// Device address of the scratch array, resolved once per device.
+double *noalloc_scratch(int device) {
+  static std::mutex mu;
+  static std::vector<double *> addr;
+  std::lock_guard<std::mutex> lock(mu);
+  if ((int)addr.size() <= device) addr.resize(device + 1, nullptr);
+  if (!addr[device]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return nullptr;
+    int optin = 0;
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess) return nullptr;
+    if (cudaFuncSetAttribute((const void *)k_matvec_noalloc<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             optin - 8192) != cudaSuccess ||
+        cudaFuncSetAttribute((const void *)k_matvec_noalloc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             optin - 8192) != cudaSuccess)
+      return nullptr;
+    addr[device] = static_cast<double *>(p);
+  }
+  return addr[device];
+}
+
+}  // namespace detail
+}  // namespace cfem
+
+extern "C" cfem_status cfem_matvec_energy_noalloc(cfem_ctx *ctx, const double *x, double *y, double *energy) {
+  using namespace cfem::detail;
+  if (!ctx || !x || !y) {
+    g_last_error = "cfem_matvec_energy_noalloc: null argument";
+    return CFEM_ERR_INVALID_ARGUMENT;
+  }
+  (void)cudaGetLastError();
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev != ctx->device) {
+    g_last_error = "cfem_matvec_energy_noalloc: the context's device must be current";
+    return CFEM_ERR_INVALID_ARGUMENT;
+  }
+  if (ctx->grid_mv > kNoAllocMaxBlocks) {
+    g_last_error = "cfem_matvec_energy_noalloc: the context needs " + std::to_string(ctx->grid_mv) +
+                   " blocks, more than the " + std::to_string(kNoAllocMaxBlocks) + " the fixed scratch holds";
+    return CFEM_ERR_INVALID_ARGUMENT;
+  }
+  double *scratch = noalloc_scratch(dev);
+  if (!scratch) {
+    g_last_error = "cfem_matvec_energy_noalloc: cudaGetSymbolAddress of the scratch array failed";
+    return CFEM_ERR_CUDA;
+  }
+  cudaStream_t s = ctx->stream;
+  if (ctx->own_stream) {
+    if (cudaEventRecord(ctx->ev_in, ctx->user_stream) != cudaSuccess || cudaStreamWaitEvent(s, ctx->ev_in, 0) != cudaSuccess) {
+      g_last_error = "cfem_matvec_energy_noalloc: cannot order after the caller's stream";
+      return CFEM_ERR_CUDA;
+    }
+  }
+  // y accumulates and the ticket counter must start at zero
+  if (cudaMemsetAsync(y, 0, sizeof(double) * ctx->nd, s) != cudaSuccess ||
+      cudaMemsetAsync(scratch + kNoAllocCounter, 0, sizeof(double), s) != cudaSuccess) {
+    g_last_error = "cfem_matvec_energy_noalloc: cudaMemsetAsync failed";
+    return CFEM_ERR_CUDA;
+  }
+  MvParams<double> P = base_mv_d(ctx);
+  P.diagA = ctx->diagK.p;
+  if (ctx->dim == 3)
+    k_matvec_noalloc<3><<<ctx->grid_mv, kThreads, ctx->smem64, s>>>(P, x, y, ctx->node_new2old.p, scratch);
+  else
+    k_matvec_noalloc<2><<<ctx->grid_mv, kThreads, ctx->smem64, s>>>(P, x, y, ctx->node_new2old.p, scratch);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && energy)
+    e = cudaMemcpyAsync(energy, scratch + kNoAllocResult, sizeof(double), cudaMemcpyDefault, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    g_last_error = std::string("cfem_matvec_energy_noalloc: ") + cudaGetErrorString(e);
+    return CFEM_ERR_CUDA;
+  }
+  return CFEM_OK;
+}

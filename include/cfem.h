@@ -240,6 +240,23 @@ CFEM_API cfem_status cfem_element_stress(cfem_ctx *ctx, const double *u, double 
 CFEM_API cfem_status cfem_dyn_adjoint(cfem_ctx *ctx, const cfem_dyn_params *prm, const cfem_wavelet *w, int32_t n_rec,
                                       const int32_t *rec_nodes, const double *obs, double *loss, double *dLdE,
                                       cfem_dyn_info *info);
+/* y = K' x and *energy = x.K'x for callers that cannot allocate device memory:
+ * code that runs inside another framework's memory pool (an allocator that owns
+ * the whole device), or in a loop that must not hit the implicit device-wide
+ * synchronisation of cudaMalloc / cudaFree. This call allocates nothing: x and
+ * y are the caller's device arrays ([n_nodes][dim] FP64, caller node order),
+ * energy points to one double in host or device memory (may be NULL), and the
+ * only scratch is a fixed array compiled into the library (per-block partial
+ * sums for at most CFEM_NOALLOC_MAX_BLOCKS blocks, about 33 KB, held on every
+ * GPU that loads the library until the process exits). A context that needs
+ * more blocks is rejected with CFEM_ERR_INVALID_ARGUMENT. The first call on a
+ * device resolves the scratch address there; make that first call outside any
+ * stream capture. All calls share the one scratch array, so calls that overlap
+ * on the GPU (other streams, other threads, other contexts) race and must be
+ * serialised by the caller. This entry point has no counterpart in the
+ * reference. */
+#define CFEM_NOALLOC_MAX_BLOCKS 4096
+CFEM_API cfem_status cfem_matvec_energy_noalloc(cfem_ctx *ctx, const double *x, double *y, double *energy);
 /* Per-element Young's modulus update (keeps geometry; rebuilds operator scale). */
 CFEM_API cfem_status cfem_set_young(cfem_ctx *ctx, const double *elem_young);
 
