@@ -32,6 +32,10 @@ MvParams<T> base_mv_t(cfem_ctx *c) {
   P.cK = 1;
   P.cM = 0;
   P.partials = c->partials.p;
+  P.inc = c->inc.p;
+  P.inc_start = c->inc_start.p;
+  P.pe = c->prep.patch_elems;
+  P.np_max = c->np_slots;
   return P;
 }
 
@@ -356,6 +360,8 @@ void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, co
   CK(cudaGetDevice(&c->device));
   CK(cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, c->device));
   int pe = opt && opt->patch_elems > 0 ? opt->patch_elems : 512;
+  // whole warp rounds; the per-incidence force slots of a patch must fit in shared memory
+  pe = std::min(std::max((pe + 31) / 32 * 32, 32), m && m->dim == 2 ? 2048 : 1024);
   std::string err = build_prep(*m, pe, c->prep);
   if (!err.empty()) throw Fail{CFEM_ERR_MESH, err};
   err = build_rhs(*m, c->prep, c->semantics, c->rhs);
@@ -377,6 +383,13 @@ void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, co
   c->elem_new2old.upload(P.elem_new2old.data(), P.elem_new2old.size(), s);
   c->elem_old2new.upload(P.elem_old2new.data(), P.elem_old2new.size(), s);
   c->lconn.upload(reinterpret_cast<const uint2 *>(P.lconn.data()), (size_t)c->ne, s);
+  {
+    // incidence codes padded so the last patch's 16-byte copies stay inside
+    std::vector<uint16_t> ic(P.inc);
+    ic.resize((size_t)((c->ne + 1) / 2 * 2) * 4 + 8, 0);
+    c->inc.upload(ic.data(), ic.size(), s);
+    c->inc_start.upload(P.inc_start.data(), P.inc_start.size(), s);
+  }
   c->bits.upload(P.node_bits.data(), P.node_bits.size(), s);
   // coordinates and global connectivity in the new order (setup + checks)
   {
@@ -418,8 +431,9 @@ void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, co
   k_convert<double, float><<<nblk(c->nvec), kThreads, 0, s>>>(c->nvec, c->FB.p, c->FB32.p);
   CKL();
   // launch shapes
-  c->smem64 = (size_t)P.np_max * c->vw * 2 * sizeof(double);
-  c->smem32 = (size_t)P.np_max * c->vw * 2 * sizeof(float);
+  c->np_slots = (P.np_max + 3) / 4 * 4;
+  c->smem64 = matvec_smem_bytes(c->dim, sizeof(double), P.patch_elems, c->np_slots);
+  c->smem32 = matvec_smem_bytes(c->dim, sizeof(float), P.patch_elems, c->np_slots);
   // The limit is an attribute of the kernel function (shared by every context
   // in the process), so it is raised once to the device maximum; each launch
   // still requests only its own patch size.

@@ -106,6 +106,8 @@ struct cfem_ctx {
   // mesh on device
   DBuf<int32_t> elem_off, node_off, nodes, own, node_new2old, elem_new2old, elem_old2new, conn;
   DBuf<uint2> lconn;
+  DBuf<uint16_t> inc, inc_start;  // per-patch incidence lists
+  int np_slots = 0;               // node slots per patch in shared memory
   DBuf<uint8_t> bits;
   DBuf<double> coords, escale, young_d;
   // operator

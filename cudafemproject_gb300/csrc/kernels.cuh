@@ -230,27 +230,45 @@ struct MvParams {
   Scalars *sc;       // PCG scalars (beta in, sigma out)
   double *partials;  // [gridDim] partial sums of p.Ap
   T c1, c2;          // DYN: d_new = d + c1 v + c2 a
+  const uint16_t *inc, *inc_start;  // per-patch incidence lists (prep.hpp)
+  int pe, np_max;    // element slots per patch, node slots per patch (multiple of 4)
 };
 
+// One CTA per patch (grid-stride over patches). Three phases per patch:
+//  1. stage: the patch's node values (PCG: p = z + beta p_old, written back for
+//     the nodes the patch owns; DYN: the predictor), constrained DOFs zeroed;
+//     the patch's incidence lists are copied next to them;
+//  2. elements: one thread per element computes its nodal forces from the
+//     scaled gradients and stores them with plain stores into its own slots
+//     fs[a][le] (no atomics, conflict-free: consecutive threads, consecutive slots);
+//  3. nodes: one thread per patch node sums its incidences in a fixed order,
+//     masks constrained DOFs / adds the (I - P) diag term on owned nodes, and
+//     adds the result into y (global atomics: a node can be in several patches).
 template <typename T, int DIM, int MODE>
 __global__ void __launch_bounds__(kThreads) k_matvec(MvParams<T> P) {
   constexpr int VW = DIM == 3 ? 4 : 2;
+  constexpr int NV = DIM + 1;
   constexpr int NC = DIM * DIM;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  // sp: staged node values, VW per node (one 16/32-byte shared load per node);
-  // sy: accumulators, structure of arrays (bank = node index mod 32)
-  T *sp = reinterpret_cast<T *>(smem_raw);
+  T *sp = reinterpret_cast<T *>(smem_raw);                                     // [np_max][VW]
+  T *fs = sp + (size_t)P.np_max * VW;                                          // [NV][pe][VW]
+  uint16_t *si = reinterpret_cast<uint16_t *>(fs + (size_t)NV * P.pe * VW);  // [4 pe] codes
+  uint16_t *ss = si + 4 * P.pe;                                                // [np_max + 1] starts
+  int32_t *sg = reinterpret_cast<int32_t *>(ss + ((P.np_max + 2) & ~1));       // [np_max] node ids
+  uint8_t *sb = reinterpret_cast<uint8_t *>(sg + P.np_max);                    // [np_max] BC bits
   if (MODE == MV_PCG && P.sc->done) return;
   T beta = 0;
   if (MODE == MV_PCG) beta = P.sc->iter == 0 ? T(0) : T(P.sc->gamma / P.sc->gamma_prev);
-  const int np_cap = 0;  // unused
-  (void)np_cap;
   double energy = 0;
   for (int patch = blockIdx.x; patch < P.n_patches; patch += gridDim.x) {
     const int nb = P.node_off[patch], nn = P.node_off[patch + 1] - nb, own = P.own[patch];
     const int e0 = P.elem_off[patch], ne = P.elem_off[patch + 1] - e0;
-    T *sy = sp + (size_t)nn * VW;  // [DIM][nn]
-    // stage
+    // 1. stage
+    {
+      const uint4 *src = reinterpret_cast<const uint4 *>(P.inc + (size_t)4 * e0);  // e0 is even
+      for (int q = threadIdx.x; q < (ne + 1) / 2; q += blockDim.x) reinterpret_cast<uint4 *>(si)[q] = src[q];
+      for (int i = threadIdx.x; i <= nn; i += blockDim.x) ss[i] = P.inc_start[nb + patch + i];
+    }
     for (int i = threadIdx.x; i < nn; i += blockDim.x) {
       const int g = P.nodes[nb + i];
       NodeV<T, VW> v = ldv<T, VW>(P.x, g);
@@ -272,11 +290,11 @@ __global__ void __launch_bounds__(kThreads) k_matvec(MvParams<T> P) {
 #pragma unroll
       for (int d = 0; d < VW; ++d) m.v[d] = (d < DIM && !(b >> d & 1u)) ? v.v[d] : T(0);
       stv<T, VW>(sp, i, m);
-#pragma unroll
-      for (int d = 0; d < DIM; ++d) sy[(size_t)d * nn + i] = 0;
+      sg[i] = g;
+      sb[i] = (uint8_t)b;
     }
     __syncthreads();
-    // compute
+    // 2. elements
     for (int le = threadIdx.x; le < ne; le += blockDim.x) {
       const int e = e0 + le;
       const uint2 c = P.lconn[e];
@@ -284,9 +302,9 @@ __global__ void __launch_bounds__(kThreads) k_matvec(MvParams<T> P) {
       T G[NC];
 #pragma unroll
       for (int k = 0; k < NC; ++k) G[k] = P.G[(size_t)k * P.gstride + e];
-      T u[DIM + 1][DIM], f[DIM + 1][DIM];
+      T u[NV][DIM], f[NV][DIM];
 #pragma unroll
-      for (int a = 0; a <= DIM; ++a) {
+      for (int a = 0; a < NV; ++a) {
         const NodeV<T, VW> s = ldv<T, VW>(sp, li[a]);
 #pragma unroll
         for (int d = 0; d < DIM; ++d) u[a][d] = s.v[d];
@@ -297,24 +315,37 @@ __global__ void __launch_bounds__(kThreads) k_matvec(MvParams<T> P) {
       // FP64 pipe of this part is narrow, so no per-term double arithmetic)
       T e_elem = 0;
 #pragma unroll
-      for (int a = 0; a <= DIM; ++a)
+      for (int a = 0; a < NV; ++a) {
+        NodeV<T, VW> o;
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) {
+        for (int d = 0; d < VW; ++d) o.v[d] = d < DIM ? f[a][d] : T(0);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d)
           if (MODE == MV_PCG) e_elem += u[a][d] * f[a][d];
-          atomicAdd(sy + (size_t)d * nn + li[a], f[a][d]);
-        }
+        stv<T, VW>(fs, (size_t)a * P.pe + le, o);
+      }
       if (MODE == MV_PCG) energy += (double)e_elem;
     }
     __syncthreads();
-    // flush
+    // 3. nodes
     for (int i = threadIdx.x; i < nn; i += blockDim.x) {
-      const int g = P.nodes[nb + i];
-      const unsigned b = P.bits[g];
+      const int g = sg[i];
+      const unsigned b = sb[i];
+      T acc[DIM];
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) acc[d] = 0;
+      const int k1 = ss[i + 1];
+      for (int k = ss[i]; k < k1; ++k) {
+        const unsigned code = si[k];
+        const NodeV<T, VW> f = ldv<T, VW>(fs, (size_t)(code & 3u) * P.pe + (code >> 2));
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) acc[d] += f.v[d];
+      }
       NodeV<T, VW> r;
       bool any = false;
 #pragma unroll
       for (int d = 0; d < VW; ++d) {
-        T val = (d < DIM && !(b >> d & 1u)) ? sy[(size_t)d * nn + i] : T(0);
+        T val = (d < DIM && !(b >> d & 1u)) ? acc[d < DIM ? d : 0] : T(0);
         r.v[d] = val;
         any |= val != T(0);
       }
@@ -348,6 +379,13 @@ __global__ void __launch_bounds__(kThreads) k_matvec(MvParams<T> P) {
     double v[1] = {energy};
     if (grid_sum_last<1>(v, P.partials, &P.sc->count_mv)) P.sc->sigma = v[0];
   }
+}
+
+// Shared-memory bytes of k_matvec for a patch layout.
+inline size_t matvec_smem_bytes(int dim, size_t tsize, int pe, int np_max) {
+  const int vw = dim == 3 ? 4 : 2;
+  return (size_t)np_max * vw * tsize + (size_t)(dim + 1) * pe * vw * tsize + (size_t)4 * pe * 2 +
+         (size_t)((np_max + 2) & ~1) * 2 + (size_t)np_max * 5;
 }
 
 // ------------------------------------------------------------------ PCG vector kernels

@@ -185,6 +185,24 @@ std::string build_prep(const cfem_mesh &m, int patch_elems, Prep &P) {
   }
   P.p_elem_off[P.n_patches] = (int32_t)ne;
   P.p_node_off[P.n_patches] = (int32_t)P.p_nodes.size();
+  // ---- incidence lists (counting sort of each patch's (element, vertex) pairs by node) ----
+  P.inc.assign(ne * 4, 0);
+  P.inc_start.assign(P.p_nodes.size() + P.n_patches, 0);
+  {
+    std::vector<int32_t> pos;
+    for (int p = 0; p < P.n_patches; ++p) {
+      const int64_t e0 = P.p_elem_off[p], e1 = P.p_elem_off[p + 1];
+      const int n = P.p_node_off[p + 1] - P.p_node_off[p];
+      pos.assign(n + 1, 0);
+      for (int64_t ei = e0; ei < e1; ++ei)
+        for (int a = 0; a < nv; ++a) ++pos[P.lconn[ei * 4 + a] + 1];
+      for (int i = 0; i < n; ++i) pos[i + 1] += pos[i];
+      uint16_t *st = P.inc_start.data() + P.p_node_off[p] + p;
+      for (int i = 0; i <= n; ++i) st[i] = (uint16_t)pos[i];
+      for (int64_t ei = e0; ei < e1; ++ei)
+        for (int a = 0; a < nv; ++a) P.inc[e0 * 4 + pos[P.lconn[ei * 4 + a]]++] = (uint16_t)((ei - e0) * 4 + a);
+    }
+  }
 
   // ---- constraints (datakeeper.cpp:139-171) ----
   P.dof_bc.assign(nn * dim, 0);

@@ -29,6 +29,12 @@ struct Prep {
   std::vector<int32_t> elem_new2old, elem_old2new, node_new2old, node_old2new;
   std::vector<int32_t> p_elem_off, p_node_off, p_nodes, p_own;
   std::vector<uint16_t> lconn;     // [ne][4] local node index inside the patch (new element order)
+  // Per patch, the transpose of lconn: for every patch-local node the codes
+  // le*4 + a of the (patch-local element, vertex) pairs touching it, in
+  // increasing order. inc is [ne][4] like lconn (patch p's codes start at
+  // 4*elem_off[p]); inc_start holds nn+1 offsets per patch, patch p's at
+  // node_off[p] + p.
+  std::vector<uint16_t> inc, inc_start;
   std::vector<uint8_t> node_bits;  // [nn] new order: bit d set if DOF d is constrained
   std::vector<uint8_t> dof_bc;     // [nn*dim] original order
   std::vector<int32_t> ctype;      // [nn] original order: last Constraint::Type code or 0
