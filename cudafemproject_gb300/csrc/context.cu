@@ -41,6 +41,19 @@ MvParams<T> base_mv_t(cfem_ctx *c) {
 
 template <typename T>
 void launch_mv_t(cfem_ctx *c, int mode, const MvParams<T> &P) {
+  if (c->fans && c->dim == 3) {
+    FanParams F{c->fan_off.p, c->fan_elem_off.p, c->fan_slot.p, c->finc.p, c->finc_start.p, c->fstride};
+    const T *Gf;
+    if constexpr (sizeof(T) == 8) Gf = c->Gf64.p; else Gf = c->Gf32.p;
+    const size_t smem = sizeof(T) == 8 ? c->smem_fan64 : c->smem_fan32;
+    dim3 g(c->grid_fan), b(kFanThreads);
+    if (mode == MV_PLAIN) k_matvec_fan<T, MV_PLAIN><<<g, b, smem, c->stream>>>(P, F, Gf);
+    else if (mode == MV_PCG) k_matvec_fan<T, MV_PCG><<<g, b, smem, c->stream>>>(P, F, Gf);
+    else k_matvec_fan<T, MV_DYN><<<g, b, smem, c->stream>>>(P, F, Gf);
+    CKL();
+    c->launches += 1;
+    return;
+  }
   size_t smem = sizeof(T) == 8 ? c->smem64 : c->smem32;
   dim3 g(c->grid_mv), b(kThreads);
   if (c->dim == 3) {
@@ -342,9 +355,15 @@ void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, co
   c->nd = c->nn * c->dim;
   c->nvec = c->nn * c->vw;
   c->semantics = opt ? opt->semantics : CFEM_COMPAT;
-  c->form = CFEM_FORM_GRADIENT;
-  if (opt && opt->matvec_form == CFEM_FORM_STORED_KE)
+  const int req_form = opt ? opt->matvec_form : CFEM_FORM_AUTO;
+  if (req_form == CFEM_FORM_STORED_KE)
     throw Fail{CFEM_ERR_UNSUPPORTED, "stored K_e form is not built in this library version"};
+  if (req_form < CFEM_FORM_AUTO || req_form > CFEM_FORM_GRADIENT_FAN)
+    throw Fail{CFEM_ERR_INVALID_ARGUMENT, "unknown matvec_form"};
+  if (req_form == CFEM_FORM_GRADIENT_FAN && m->dim != 3)
+    throw Fail{CFEM_ERR_INVALID_ARGUMENT, "the edge-fan form is for tetrahedra (dim 3)"};
+  c->fans = m->dim == 3 && (req_form == CFEM_FORM_AUTO || req_form == CFEM_FORM_GRADIENT_FAN);
+  c->form = c->fans ? CFEM_FORM_GRADIENT_FAN : CFEM_FORM_GRADIENT;
   c->verbose = opt ? opt->verbose : 0;
   c->E = mat ? mat->young_modulus : 2e7;
   c->nu = mat ? mat->poisson_ratio : 0.3;
@@ -359,10 +378,10 @@ void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, co
   }
   CK(cudaGetDevice(&c->device));
   CK(cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, c->device));
-  int pe = opt && opt->patch_elems > 0 ? opt->patch_elems : 512;
-  // whole warp rounds; the per-incidence force slots of a patch must fit in shared memory
-  pe = std::min(std::max((pe + 31) / 32 * 32, 32), m && m->dim == 2 ? 2048 : 1024);
-  std::string err = build_prep(*m, pe, c->prep);
+  int pe = opt && opt->patch_elems > 0 ? opt->patch_elems : (c->fans ? kFanMax * kFanThreads : 512);
+  // the per-incidence force slots of a patch must fit in shared memory
+  pe = std::min(std::max((pe + 31) / 32 * 32, 32), m->dim == 2 ? 2048 : 1024);
+  std::string err = build_prep(*m, pe, c->fans, c->prep);
   if (!err.empty()) throw Fail{CFEM_ERR_MESH, err};
   err = build_rhs(*m, c->prep, c->semantics, c->rhs);
   if (!err.empty()) throw Fail{CFEM_ERR_MESH, err};
@@ -384,11 +403,24 @@ void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, co
   c->elem_old2new.upload(P.elem_old2new.data(), P.elem_old2new.size(), s);
   c->lconn.upload(reinterpret_cast<const uint2 *>(P.lconn.data()), (size_t)c->ne, s);
   {
-    // incidence codes padded so the last patch's 16-byte copies stay inside
-    std::vector<uint16_t> ic(P.inc);
-    ic.resize((size_t)((c->ne + 1) / 2 * 2) * 4 + 8, 0);
-    c->inc.upload(ic.data(), ic.size(), s);
+    c->inc.upload(P.inc.data(), P.inc.size(), s);
     c->inc_start.upload(P.inc_start.data(), P.inc_start.size(), s);
+  }
+  if (c->fans) {
+    c->fstride = (P.n_fans + 31) / 32 * 32;
+    std::vector<uint16_t> slot((size_t)kFanSlots * c->fstride, 0);
+    for (int64_t f = 0; f < P.n_fans; ++f)
+      for (int k = 0; k < kFanSlots; ++k) slot[(size_t)k * c->fstride + f] = P.fan_slot[f * kFanSlots + k];
+    c->fan_slot.upload(slot.data(), slot.size(), s);
+    c->fan_off.upload(P.p_fan_off.data(), P.p_fan_off.size(), s);
+    c->fan_elem_off.upload(P.fan_elem_off.data(), P.fan_elem_off.size(), s);
+    c->finc.upload(P.finc.data(), P.finc.size(), s);
+    c->finc_start.upload(P.finc_start.data(), P.finc_start.size(), s);
+    std::vector<int32_t> pos(c->ne);
+    for (int64_t f = 0; f < P.n_fans; ++f)
+      for (int32_t e = P.fan_elem_off[f]; e < P.fan_elem_off[f + 1]; ++e) pos[e] = (int32_t)(f * 8 + (e - P.fan_elem_off[f]));
+    c->fan_pos.upload(pos.data(), pos.size(), s);
+    c->fan_perm.upload(P.fan_perm.data(), P.fan_perm.size(), s);
   }
   c->bits.upload(P.node_bits.data(), P.node_bits.size(), s);
   // coordinates and global connectivity in the new order (setup + checks)
@@ -464,8 +496,21 @@ void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, co
   }
   occ = std::max(occ, 1);
   c->grid_mv = (int)std::min<int64_t>(P.n_patches, (int64_t)c->n_sm * occ);
+  if (c->fans) {
+    c->smem_fan64 = fan_smem_bytes(sizeof(double), c->np_slots);
+    c->smem_fan32 = fan_smem_bytes(sizeof(float), c->np_slots);
+    if (c->smem_fan64 + 8192 > (size_t)smem_optin)
+      throw Fail{CFEM_ERR_INVALID_ARGUMENT, "fan patch too large for shared memory: lower patch_elems"};
+    for (const void *k : {(const void *)k_matvec_fan<double, MV_PLAIN>, (const void *)k_matvec_fan<double, MV_PCG>,
+                          (const void *)k_matvec_fan<double, MV_DYN>, (const void *)k_matvec_fan<float, MV_PLAIN>,
+                          (const void *)k_matvec_fan<float, MV_PCG>, (const void *)k_matvec_fan<float, MV_DYN>})
+      CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin - 8192));
+    int occf = 1;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occf, k_matvec_fan<float, MV_PCG>, kFanThreads, c->smem_fan32));
+    c->grid_fan = (int)std::min<int64_t>(P.n_patches, (int64_t)c->n_sm * std::max(occf, 1));
+  }
   c->grid_vec = (int)std::min<int64_t>(std::max<int64_t>(1, nblk(c->nn)), (int64_t)c->n_sm * 4);
-  int maxgrid = std::max(c->grid_mv, c->grid_vec);
+  int maxgrid = std::max({c->grid_mv, c->grid_vec, c->grid_fan});
   c->partials.alloc((size_t)maxgrid * 4);
   c->counters.alloc(4);
   c->counters.zero(s);
@@ -536,6 +581,17 @@ void rebuild_operator(cfem_ctx *c) {
   if (c->dim == 3) k_geometry<3><<<nblk(c->ne), kThreads, 0, s>>>(gp);
   else k_geometry<2><<<nblk(c->ne), kThreads, 0, s>>>(gp);
   CKL();
+  if (c->fans) {
+    if (!c->Gf64.p) {
+      c->Gf64.alloc((size_t)kFanMax * 9 * c->fstride);
+      c->Gf32.alloc((size_t)kFanMax * 9 * c->fstride);
+    }
+    c->Gf64.zero(s);
+    c->Gf32.zero(s);
+    k_fan_gradients<<<nblk(c->ne), kThreads, 0, s>>>(c->ne, c->G64.p, c->gstride, c->fan_pos.p, c->fan_perm.p, c->Gf64.p,
+                                                     c->Gf32.p, c->fstride);
+    CKL();
+  }
   // consistent-mass diagonal: 2 * cons_c * rho * V per DOF, assembled = mlump * 2 cons_c / lump_c
   k_axpby64<<<nblk(c->nvec), kThreads, 0, s>>>(c->nvec, 2 * cons_c / lump_c, c->mlump.p, 0.0, c->mcdiag.p);
   CKL();
@@ -660,15 +716,15 @@ cfem_status cfem_dof_map(const cfem_ctx *ctx, int32_t *mask) {
     if (!mask) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "null mask"};
     // element-local slot (caller element e, vertex a, component d) -> dim*node + d
     const Prep &P = ctx->prep;
-    for (int64_t ei = 0; ei < ctx->ne; ++ei) {
-      int64_t e = P.elem_new2old[ei];
-      for (int a = 0; a < ctx->nv; ++a) {
-        int patch = (int)(ei / P.patch_elems);
-        int g = P.p_nodes[P.p_node_off[patch] + P.lconn[ei * 4 + a]];
-        int64_t node = P.node_new2old[g];
-        for (int d = 0; d < ctx->dim; ++d) mask[e * ctx->w + ctx->dim * a + d] = (int32_t)(ctx->dim * node + d);
+    for (int patch = 0; patch < P.n_patches; ++patch)
+      for (int64_t ei = P.p_elem_off[patch]; ei < P.p_elem_off[patch + 1]; ++ei) {
+        int64_t e = P.elem_new2old[ei];
+        for (int a = 0; a < ctx->nv; ++a) {
+          int g = P.p_nodes[P.p_node_off[patch] + P.lconn[ei * 4 + a]];
+          int64_t node = P.node_new2old[g];
+          for (int d = 0; d < ctx->dim; ++d) mask[e * ctx->w + ctx->dim * a + d] = (int32_t)(ctx->dim * node + d);
+        }
       }
-    }
     return CFEM_OK;
   });
 }
@@ -679,13 +735,12 @@ cfem_status cfem_adjacency(const cfem_ctx *ctx, int32_t *adj) {
     if (!adj) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "null adj"};
     std::fill(adj, adj + ctx->nd, 0);
     const Prep &P = ctx->prep;
-    for (int64_t ei = 0; ei < ctx->ne; ++ei) {
-      int patch = (int)(ei / P.patch_elems);
-      for (int a = 0; a < ctx->nv; ++a) {
-        int64_t node = P.node_new2old[P.p_nodes[P.p_node_off[patch] + P.lconn[ei * 4 + a]]];
-        for (int d = 0; d < ctx->dim; ++d) adj[node * ctx->dim + d] += 1;
-      }
-    }
+    for (int patch = 0; patch < P.n_patches; ++patch)
+      for (int64_t ei = P.p_elem_off[patch]; ei < P.p_elem_off[patch + 1]; ++ei)
+        for (int a = 0; a < ctx->nv; ++a) {
+          int64_t node = P.node_new2old[P.p_nodes[P.p_node_off[patch] + P.lconn[ei * 4 + a]]];
+          for (int d = 0; d < ctx->dim; ++d) adj[node * ctx->dim + d] += 1;
+        }
     return CFEM_OK;
   });
 }

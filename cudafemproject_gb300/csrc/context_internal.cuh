@@ -14,6 +14,7 @@
 
 #include "../../include/cfem.h"
 #include "kernels.cuh"
+#include "kernels_fan.cuh"
 #include "prep.hpp"
 
 namespace cfem {
@@ -107,6 +108,16 @@ struct cfem_ctx {
   DBuf<int32_t> elem_off, node_off, nodes, own, node_new2old, elem_new2old, elem_old2new, conn;
   DBuf<uint2> lconn;
   DBuf<uint16_t> inc, inc_start;  // per-patch incidence lists
+  // edge-fan form (3D): fan tables, gradients in fan vertex order
+  bool fans = false;
+  int64_t fstride = 0;
+  DBuf<int32_t> fan_off, fan_elem_off, fan_pos;
+  DBuf<uint16_t> fan_slot, finc, finc_start;
+  DBuf<uint8_t> fan_perm;
+  DBuf<double> Gf64;
+  DBuf<float> Gf32;
+  size_t smem_fan64 = 0, smem_fan32 = 0;
+  int grid_fan = 0;
   int np_slots = 0;               // node slots per patch in shared memory
   DBuf<uint8_t> bits;
   DBuf<double> coords, escale, young_d;

@@ -265,8 +265,8 @@ __global__ void __launch_bounds__(kThreads) k_matvec(MvParams<T> P) {
     const int e0 = P.elem_off[patch], ne = P.elem_off[patch + 1] - e0;
     // 1. stage
     {
-      const uint4 *src = reinterpret_cast<const uint4 *>(P.inc + (size_t)4 * e0);  // e0 is even
-      for (int q = threadIdx.x; q < (ne + 1) / 2; q += blockDim.x) reinterpret_cast<uint4 *>(si)[q] = src[q];
+      const uint2 *src = reinterpret_cast<const uint2 *>(P.inc + (size_t)4 * e0);  // 4 codes per element
+      for (int q = threadIdx.x; q < ne; q += blockDim.x) reinterpret_cast<uint2 *>(si)[q] = src[q];
       for (int i = threadIdx.x; i <= nn; i += blockDim.x) ss[i] = P.inc_start[nb + patch + i];
     }
     for (int i = threadIdx.x; i < nn; i += blockDim.x) {

@@ -1,6 +1,8 @@
 // Host-side mesh preparation; see prep.hpp.
 #include "prep.hpp"
 
+#include <array>
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -32,7 +34,7 @@ inline uint64_t spread2(uint64_t v) {  // 32 bits -> every second bit
 
 }  // namespace
 
-std::string build_prep(const cfem_mesh &m, int patch_elems, Prep &P) {
+std::string build_prep(const cfem_mesh &m, int patch_elems, bool use_fans, Prep &P) {
   const int dim = m.dim;
   if (dim != 2 && dim != 3) return "dim must be 2 or 3";
   if (m.n_nodes <= 0 || m.n_elems <= 0) return "mesh has no nodes or no elements";
@@ -92,44 +94,150 @@ std::string build_prep(const cfem_mesh &m, int patch_elems, Prep &P) {
   key.clear();
   key.shrink_to_fit();
 
-  // ---- patches; inside a patch, order elements in rounds of 32 that share no
-  // node, so one warp's shared-memory accumulations hit distinct addresses ----
+  // ---- edge fans (3D): chains of up to kFanMax tets around one edge ----
+  // Greedy in locality order: the seed tet takes the edge of its own with the
+  // most unassigned tets around it, and the unassigned tets around that edge
+  // are chained through their shared faces, starting from the seed. Tet j of a
+  // fan is {P, Q, R_j, R_j+1}; a closed ring has R_len == R_0. Without fans
+  // every element is its own fan of length 1.
   const int pe = patch_elems;
-  P.n_patches = (int)((ne + pe - 1) / pe);
-  {
-    std::vector<int32_t> stamp(nn, -1), group, rest, order;
-    int round_id = 0;
-    for (int p = 0; p < P.n_patches; ++p) {
-      int64_t e0 = (int64_t)p * pe, e1 = std::min<int64_t>(ne, e0 + pe);
-      rest.assign(P.elem_new2old.begin() + e0, P.elem_new2old.begin() + e1);
-      order.clear();
-      while (!rest.empty()) {
-        group.clear();
-        ++round_id;
-        size_t keep = 0;
-        for (size_t i = 0; i < rest.size(); ++i) {
-          const int32_t e = rest[i];
-          bool clash = false;
-          if (group.size() < 32)
-            for (int a = 0; a < nv && !clash; ++a) clash = stamp[m.elems[(int64_t)e * nv + a]] == round_id;
-          if (group.size() < 32 && !clash) {
-            group.push_back(e);
-            for (int a = 0; a < nv; ++a) stamp[m.elems[(int64_t)e * nv + a]] = round_id;
-          } else {
-            rest[keep++] = e;
-          }
-        }
-        rest.resize(keep);
-        // a round that cannot be filled node-disjointly is topped up in order
-        while (group.size() < 32 && !rest.empty()) {
-          group.push_back(rest.front());
-          rest.erase(rest.begin());
-        }
-        order.insert(order.end(), group.begin(), group.end());
-      }
-      std::copy(order.begin(), order.end(), P.elem_new2old.begin() + e0);
+  P.fan_elem_off.clear();
+  P.fan_ring.clear();
+  P.fan_perm.assign(ne, 0);
+  if (use_fans && dim == 3) {
+    // node -> tets (counting sort)
+    std::vector<int32_t> nt_off(nn + 1, 0), nt(ne * 4);
+    for (int64_t i = 0; i < ne * 4; ++i) ++nt_off[m.elems[i] + 1];
+    for (int64_t i = 0; i < nn; ++i) nt_off[i + 1] += nt_off[i];
+    {
+      std::vector<int32_t> pos(nt_off.begin(), nt_off.end() - 1);
+      for (int64_t e = 0; e < ne; ++e)
+        for (int a = 0; a < 4; ++a) nt[pos[m.elems[e * 4 + a]]++] = (int32_t)e;
     }
-    for (int64_t i = 0; i < ne; ++i) P.elem_old2new[P.elem_new2old[i]] = (int32_t)i;
+    std::vector<uint8_t> taken(ne, 0);
+    std::vector<int32_t> order;
+    order.reserve(ne);
+    P.fan_elem_off.push_back(0);
+    static const int kEdge[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+    std::vector<int32_t> around, best, chain;
+    for (int64_t i = 0; i < ne; ++i) {
+      const int32_t t = P.elem_new2old[i];
+      if (taken[t]) continue;
+      const int32_t *vt = m.elems + (int64_t)t * 4;
+      int best_k = 0;
+      best.clear();
+      for (int k = 0; k < 6; ++k) {
+        const int32_t p = vt[kEdge[k][0]], q = vt[kEdge[k][1]];
+        around.clear();
+        for (int32_t j = nt_off[p]; j < nt_off[p + 1]; ++j) {
+          const int32_t s = nt[j];
+          if (taken[s]) continue;
+          const int32_t *vs = m.elems + (int64_t)s * 4;
+          if (vs[0] == q || vs[1] == q || vs[2] == q || vs[3] == q) around.push_back(s);
+        }
+        if (around.size() > best.size()) { best = around; best_k = k; }
+      }
+      const int32_t p = vt[kEdge[best_k][0]], q = vt[kEdge[best_k][1]];
+      auto others = [&](int32_t s, int32_t &x, int32_t &y) {
+        const int32_t *vs = m.elems + (int64_t)s * 4;
+        x = -1; y = -1;
+        for (int a = 0; a < 4; ++a)
+          if (vs[a] != p && vs[a] != q) { if (x < 0) x = vs[a]; else y = vs[a]; }
+      };
+      auto in_chain = [&](int32_t s) { return std::find(chain.begin(), chain.end(), s) != chain.end(); };
+      chain.assign(1, t);
+      int32_t left, right;
+      others(t, left, right);
+      bool closed = false;
+      // extend through R_right, then (if still open) backwards through R_left
+      while ((int)chain.size() < kFanMax && !closed) {
+        int32_t next = -1, nv2 = -1;
+        for (int32_t s : best) {
+          if (in_chain(s)) continue;
+          int32_t x, y;
+          others(s, x, y);
+          if (x == right) { next = s; nv2 = y; break; }
+          if (y == right) { next = s; nv2 = x; break; }
+        }
+        if (next < 0) break;
+        chain.push_back(next);
+        right = nv2;
+        if (right == left) closed = true;
+      }
+      while ((int)chain.size() < kFanMax && !closed) {
+        int32_t prev = -1, nv2 = -1;
+        for (int32_t s : best) {
+          if (in_chain(s)) continue;
+          int32_t x, y;
+          others(s, x, y);
+          if (x == left) { prev = s; nv2 = y; break; }
+          if (y == left) { prev = s; nv2 = x; break; }
+        }
+        if (prev < 0) break;
+        chain.insert(chain.begin(), prev);
+        left = nv2;
+      }
+      // ring vertices R_0..R_len: walk the chain from the left end
+      const int len = (int)chain.size();
+      std::array<int32_t, kFanMax + 3> ring{};
+      ring[0] = p;
+      ring[1] = q;
+      int32_t cur = left;
+      for (int j = 0; j < len; ++j) {
+        int32_t x, y;
+        others(chain[j], x, y);
+        ring[2 + j] = cur;
+        cur = x == cur ? y : x;
+      }
+      ring[2 + len] = cur;
+      for (int j = 0; j < len; ++j) {
+        const int32_t s = chain[j];
+        taken[s] = 1;
+        const int32_t *vs = m.elems + (int64_t)s * 4;
+        const int32_t fv[4] = {p, q, ring[2 + j], ring[3 + j]};
+        uint8_t perm = 0;
+        for (int bb = 0; bb < 4; ++bb) {
+          int a = 0;
+          while (a < 4 && vs[a] != fv[bb]) ++a;
+          if (a == 4) return "internal error: edge fan does not match its tets";
+          perm |= (uint8_t)(a << (2 * bb));
+        }
+        P.fan_perm[s] = perm;  // indexed by old id here, permuted to the new order below
+        order.push_back(s);
+      }
+      for (int k = 0; k < kFanMax + 3; ++k) P.fan_ring.push_back(k < len + 3 ? ring[k] : ring[2 + len]);
+      P.fan_elem_off.push_back((int32_t)order.size());
+    }
+    std::vector<uint8_t> perm_new(ne);
+    for (int64_t i = 0; i < ne; ++i) {
+      P.elem_new2old[i] = order[i];
+      P.elem_old2new[order[i]] = (int32_t)i;
+      perm_new[i] = P.fan_perm[order[i]];
+    }
+    P.fan_perm.swap(perm_new);
+  } else {
+    P.fan_elem_off.resize(ne + 1);
+    for (int64_t i = 0; i <= ne; ++i) P.fan_elem_off[i] = (int32_t)i;
+  }
+  P.n_fans = (int64_t)P.fan_elem_off.size() - 1;
+  P.fans = use_fans && dim == 3;
+  // ---- patches: consecutive fans, at most patch_elems elements and kFanThreads fans each ----
+  P.p_elem_off.clear();
+  P.p_fan_off.clear();
+  {
+    int64_t f = 0;
+    while (f < P.n_fans) {
+      P.p_fan_off.push_back((int32_t)f);
+      P.p_elem_off.push_back(P.fan_elem_off[f]);
+      int64_t f1 = f;
+      while (f1 < P.n_fans && (f1 - f) < (P.fans ? kFanThreads : pe) &&
+             P.fan_elem_off[f1 + 1] - P.fan_elem_off[f] <= pe)
+        ++f1;
+      f = f1;
+    }
+    P.n_patches = (int)P.p_fan_off.size();
+    P.p_fan_off.push_back((int32_t)P.n_fans);
+    P.p_elem_off.push_back((int32_t)ne);
   }
   P.node_old2new.assign(nn, -1);
   P.node_new2old.resize(nn);
@@ -137,8 +245,7 @@ std::string build_prep(const cfem_mesh &m, int patch_elems, Prep &P) {
   std::vector<int32_t> first_new(P.n_patches + 1, 0);
   for (int p = 0; p < P.n_patches; ++p) {
     first_new[p] = next;
-    int64_t e1 = std::min<int64_t>(ne, (int64_t)(p + 1) * pe);
-    for (int64_t ei = (int64_t)p * pe; ei < e1; ++ei) {
+    for (int64_t ei = P.p_elem_off[p]; ei < P.p_elem_off[p + 1]; ++ei) {
       int64_t e = P.elem_new2old[ei];
       for (int a = 0; a < nv; ++a) {
         int32_t o = m.elems[e * nv + a];
@@ -151,18 +258,21 @@ std::string build_prep(const cfem_mesh &m, int patch_elems, Prep &P) {
     }
   }
   first_new[P.n_patches] = next;
-  P.p_elem_off.resize(P.n_patches + 1);
   P.p_node_off.resize(P.n_patches + 1);
   P.p_own.resize(P.n_patches);
   P.p_nodes.clear();
   P.p_nodes.reserve((size_t)(nn * 1.6) + 16);
   P.lconn.assign(ne * 4, 0);
+  if (P.fans) {
+    P.fan_slot.assign(P.n_fans * kFanSlots, 0);
+    for (int64_t f = 0; f < P.n_fans; ++f)
+      P.fan_slot[f * kFanSlots + kFanSlots - 1] = (uint16_t)(P.fan_elem_off[f + 1] - P.fan_elem_off[f]);
+  }
   std::vector<int32_t> mark(nn, -1), loc(nn, 0);
   std::vector<int32_t> list;
   P.np_max = 0;
   for (int p = 0; p < P.n_patches; ++p) {
-    int64_t e0 = (int64_t)p * pe, e1 = std::min<int64_t>(ne, e0 + pe);
-    P.p_elem_off[p] = (int32_t)e0;
+    const int64_t e0 = P.p_elem_off[p], e1 = P.p_elem_off[p + 1];
     list.clear();
     for (int64_t ei = e0; ei < e1; ++ei) {
       int64_t e = P.elem_new2old[ei];
@@ -182,8 +292,11 @@ std::string build_prep(const cfem_mesh &m, int patch_elems, Prep &P) {
       int64_t e = P.elem_new2old[ei];
       for (int a = 0; a < nv; ++a) P.lconn[ei * 4 + a] = (uint16_t)loc[P.node_old2new[m.elems[e * nv + a]]];
     }
+    if (P.fans)
+      for (int64_t f = P.p_fan_off[p]; f < P.p_fan_off[p + 1]; ++f)
+        for (int k = 0; k < kFanMax + 3; ++k)
+          P.fan_slot[f * kFanSlots + k] = (uint16_t)loc[P.node_old2new[P.fan_ring[f * (kFanMax + 3) + k]]];
   }
-  P.p_elem_off[P.n_patches] = (int32_t)ne;
   P.p_node_off[P.n_patches] = (int32_t)P.p_nodes.size();
   // ---- incidence lists (counting sort of each patch's (element, vertex) pairs by node) ----
   P.inc.assign(ne * 4, 0);
@@ -201,6 +314,29 @@ std::string build_prep(const cfem_mesh &m, int patch_elems, Prep &P) {
       for (int i = 0; i <= n; ++i) st[i] = (uint16_t)pos[i];
       for (int64_t ei = e0; ei < e1; ++ei)
         for (int a = 0; a < nv; ++a) P.inc[e0 * 4 + pos[P.lconn[ei * 4 + a]]++] = (uint16_t)((ei - e0) * 4 + a);
+    }
+  }
+  // ---- fan incidence lists: codes fl*16 + slot (slot 0 = P, 1 = Q, 2 + k = R_k) ----
+  if (P.fans) {
+    P.finc.assign(P.n_fans * kFanSlots, 0);
+    P.finc_start.assign(P.p_nodes.size() + P.n_patches, 0);
+    std::vector<int32_t> pos;
+    for (int p = 0; p < P.n_patches; ++p) {
+      const int64_t f0 = P.p_fan_off[p], f1 = P.p_fan_off[p + 1];
+      const int n = P.p_node_off[p + 1] - P.p_node_off[p];
+      pos.assign(n + 1, 0);
+      for (int64_t f = f0; f < f1; ++f) {
+        const int len = P.fan_slot[f * kFanSlots + kFanSlots - 1];
+        for (int k = 0; k < len + 3; ++k) ++pos[P.fan_slot[f * kFanSlots + k] + 1];
+      }
+      for (int i = 0; i < n; ++i) pos[i + 1] += pos[i];
+      uint16_t *st = P.finc_start.data() + P.p_node_off[p] + p;
+      for (int i = 0; i <= n; ++i) st[i] = (uint16_t)pos[i];
+      for (int64_t f = f0; f < f1; ++f) {
+        const int len = P.fan_slot[f * kFanSlots + kFanSlots - 1];
+        for (int k = 0; k < len + 3; ++k)
+          P.finc[f0 * kFanSlots + pos[P.fan_slot[f * kFanSlots + k]]++] = (uint16_t)((f - f0) * 16 + k);
+      }
     }
   }
 

@@ -20,6 +20,12 @@
 
 namespace cfem {
 
+// Edge fans: at most kFanMax tets sharing one edge, evaluated by one thread;
+// a patch holds at most kFanThreads fans (one CTA of that many threads).
+constexpr int kFanMax = 6;
+constexpr int kFanSlots = kFanMax + 4;  // P, Q, R_0..R_kFanMax, length
+constexpr int kFanThreads = 128;
+
 struct Prep {
   int dim = 0, nv = 0, w = 0;
   int64_t nn = 0, ne = 0;
@@ -35,13 +41,27 @@ struct Prep {
   // 4*elem_off[p]); inc_start holds nn+1 offsets per patch, patch p's at
   // node_off[p] + p.
   std::vector<uint16_t> inc, inc_start;
+  // Edge fans (3D, when requested). Elements are numbered fan by fan: fan f
+  // holds elements fan_elem_off[f] .. fan_elem_off[f+1]-1, element j of it
+  // being {P, Q, R_j, R_j+1}. fan_slot[f][0..kFanMax+2] are the patch-local
+  // node indices of P, Q, R_0..R_kFanMax (unused tail repeats the last ring
+  // vertex) and fan_slot[f][kFanSlots-1] the fan length. fan_perm[e] packs,
+  // two bits per fan vertex b, which vertex of the element's own connectivity
+  // it is. finc / finc_start: per patch the incidence lists of the fan slots
+  // (codes fl*16 + slot, fl the patch-local fan), laid out like inc / inc_start
+  // with patch p's codes starting at kFanSlots*p_fan_off[p].
+  bool fans = false;
+  int64_t n_fans = 0;
+  std::vector<int32_t> fan_elem_off, p_fan_off, fan_ring;
+  std::vector<uint8_t> fan_perm;
+  std::vector<uint16_t> fan_slot, finc, finc_start;
   std::vector<uint8_t> node_bits;  // [nn] new order: bit d set if DOF d is constrained
   std::vector<uint8_t> dof_bc;     // [nn*dim] original order
   std::vector<int32_t> ctype;      // [nn] original order: last Constraint::Type code or 0
 };
 
 // Returns an empty string on success, else the error message.
-std::string build_prep(const cfem_mesh &m, int patch_elems, Prep &out);
+std::string build_prep(const cfem_mesh &m, int patch_elems, bool use_fans, Prep &out);
 
 // Wavelet value in the reference's float arithmetic (fem_utils.cpp:53-82).
 float wavelet_value(const cfem_wavelet *w, float t);

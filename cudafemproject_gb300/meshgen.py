@@ -119,6 +119,35 @@ def box_3d(nx: int, ny: int, nz: int, lx: float = 1.0, ly: float = 1.0, lz: floa
                    E=E, nu=nu, rho=rho)
 
 
+def random_tets(n_points: int = 800, seed: int = 7, E: float = 2e7, nu: float = 0.25, rho: float = 2000.0) -> Problem:
+    """Unstructured tets: Delaunay tetrahedralisation (scipy) of uniform random
+    points in the 1x1x4 box, slivers removed. Nodes with z < 0.3 are clamped (type 7); nodes
+    with z > 3.7 carry a point load (0, -1e3, 0). Tet orientation as returned."""
+    from scipy.spatial import Delaunay
+    rng = np.random.default_rng(seed)
+    nodes = rng.random((n_points, 3)) * np.array([1.0, 1.0, 4.0])
+    elems = Delaunay(nodes).simplices.astype(np.int32)
+    # drop slivers (quality 6 sqrt(2) V / l_max^3 below 0.1): they only add
+    # rounding noise; the remaining mesh is still conforming (with voids)
+    X = nodes[elems]
+    vol = np.abs(np.einsum("ij,ij->i", X[:, 1] - X[:, 0], np.cross(X[:, 2] - X[:, 0], X[:, 3] - X[:, 0]))) / 6
+    edges = [(0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3)]
+    lmax = np.max([np.linalg.norm(X[:, a] - X[:, b], axis=1) for a, b in edges], axis=0)
+    elems = elems[6 * np.sqrt(2) * vol / lmax ** 3 >= 0.1]
+    used = np.zeros(n_points, bool)
+    used[elems.ravel()] = True
+    remap = np.cumsum(used) - 1
+    nodes = nodes[used]
+    elems = remap[elems].astype(np.int32)
+    clamp = np.nonzero(nodes[:, 2] < 0.3)[0].astype(np.int32)
+    cons = np.stack([clamp, np.full(len(clamp), 7, np.int32)], axis=1).astype(np.int32)
+    top = np.nonzero(nodes[:, 2] > 3.7)[0].astype(np.int32)
+    load_vec = np.tile(np.array([0.0, -1e3, 0.0]), (len(top), 1))
+    return Problem(dim=3, nodes=nodes, elems=elems, cons=cons, load_node=top, load_vec=load_vec,
+                   face_nodes=np.zeros((0, 4), np.int32), face_elem=np.zeros(0, np.int32),
+                   face_normal=np.zeros((0, 3)), face_pressure=np.zeros(0), E=E, nu=nu, rho=rho)
+
+
 def cantilever_1p39m(seed: int = 0) -> Problem:
     """1x1x4 box, 48x48x192 hexes x 6 tets (2,654,208 tets, 1,390,179 DOF), jitter 0.2h."""
     return box_3d(48, 48, 192, jitter=0.2, seed=seed, traction=(0.0, -1e3, 0.0))

@@ -45,7 +45,7 @@ class FemContext:
     reference, quirks included) or "consistent" (textbook operators/loads)."""
 
     def __init__(self, p: Problem, semantics: str = "compat", stream=None, patch_elems: int = 0,
-                 verbose: bool = False, matvec_form: str = "gradient"):
+                 verbose: bool = False, matvec_form: str = "auto"):
         self.p = p
         self.dim = p.dim
         self.n_nodes = p.n_nodes
@@ -67,7 +67,8 @@ class FemContext:
                          len(k["lnode"]), pz(k["lnode"]), pz(k["lvec"]), len(k["felem"]), pz(k["fnodes"]),
                          pz(k["felem"]), pz(k["fnorm"]), pz(k["fpress"]), pz(k["young"]))
         mat = capi.Material(float(p.E), float(p.nu), float(p.rho))
-        form = {"gradient": capi.FORM_GRADIENT, "stored_ke": capi.FORM_STORED_KE, "auto": capi.FORM_AUTO}[matvec_form]
+        form = {"gradient": capi.FORM_GRADIENT, "stored_ke": capi.FORM_STORED_KE, "auto": capi.FORM_AUTO,
+                "fan": capi.FORM_GRADIENT_FAN}[matvec_form]
         opt = capi.Options({"compat": capi.COMPAT, "consistent": capi.CONSISTENT}[semantics], form, int(patch_elems),
                            int(verbose))
         h = C.c_void_p()

@@ -165,15 +165,40 @@ def test_square_2d_64_fp64_vs_oracle():
     assert rel(u2, xo) <= 1e-10
 
 
-def test_jittered_box_patch_sizes():
-    """Results do not depend on the CTA patch size (locality layout only)."""
+@pytest.mark.parametrize("form", ["gradient", "fan"])
+def test_jittered_box_patch_sizes(form):
+    """Results do not depend on the CTA patch size or on the element grouping
+    (per element or per edge fan): locality layout only."""
     from cudafemproject_gb300.solver import FemContext
     p = meshgen.box_3d(6, 5, 14, jitter=0.2, seed=11)
     o = O.Oracle(p)
     xo, _ = o.static(tol=1e-14, rule=1)
     for pe in (64, 256, 1024):
-        u, _ = FemContext(p, patch_elems=pe).static_solve("fp64", tol=1e-14, stop_rule="residual")
+        ctx = FemContext(p, patch_elems=pe, matvec_form=form)
+        assert ctx.counts()["matvec_form"] == {"gradient": 1, "fan": 3}[form]
+        u, _ = ctx.static_solve("fp64", tol=1e-14, stop_rule="residual")
         assert rel(u, xo) <= 1e-10, pe
+
+
+@pytest.mark.parametrize("form", ["gradient", "fan"])
+@pytest.mark.parametrize("pe", [96, 768])
+def test_unstructured_tets_both_forms(form, pe):
+    """Delaunay mesh of random points: edge fans of every length 1..6, open and
+    closed. Matvec and FP64 / refined solves against the oracle."""
+    from cudafemproject_gb300.solver import FemContext
+    p = meshgen.random_tets(800, seed=7)
+    o = O.Oracle(p, consistent=True)
+    ctx = FemContext(p, semantics="consistent", patch_elems=pe, matvec_form=form)
+    rng = np.random.default_rng(2)
+    x = rng.standard_normal(p.n_dof)
+    assert rel(ctx.matvec(x, "fp64"), o.matvec(x)) < 1e-13
+    y32 = ctx.matvec(x.astype(np.float32), "fp32")
+    assert rel(y32, o.matvec(x.astype(np.float32).astype(np.float64))) < 2e-6
+    xo, _ = o.static(tol=1e-14, rule=1)
+    u, info = ctx.static_solve("fp64", tol=1e-14, stop_rule="residual")
+    assert rel(u, xo) <= 1e-9
+    u2, info2 = ctx.static_solve("fp32_refine", tol=1e-4, stop_rule="residual", outer_tol=1e-12)
+    assert rel(u2, xo) <= 1e-8
 
 
 def test_consistent_static(ctxs):
