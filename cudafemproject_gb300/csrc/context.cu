@@ -41,6 +41,26 @@ MvParams<T> base_mv_t(cfem_ctx *c) {
 
 template <typename T>
 void launch_mv_t(cfem_ctx *c, int mode, const MvParams<T> &P) {
+  // FP32: patch blocks streamed by bulk copies. FP64 keeps the plain fan
+  // kernel below: it is bound by the FP64 pipe, and its twice-as-large blocks
+  // would leave one CTA per SM.
+  if constexpr (sizeof(T) == 4) {
+    if (c->fans && c->fan_tma) {
+      FanTmaParams F{};
+      F.blocks = c->blk32.p;
+      F.L = c->L32;
+      F.fan_off = c->fan_off.p;
+      F.fan_elem_off = c->fan_elem_off.p;
+      F.err = c->tma_err.p;
+      dim3 g(c->grid_ft32), b(kFanThreads);
+      if (mode == MV_PLAIN) k_matvec_fan_tma<float, MV_PLAIN><<<g, b, c->smem_ft32, c->stream>>>(P, F);
+      else if (mode == MV_PCG) k_matvec_fan_tma<float, MV_PCG><<<g, b, c->smem_ft32, c->stream>>>(P, F);
+      else k_matvec_fan_tma<float, MV_DYN><<<g, b, c->smem_ft32, c->stream>>>(P, F);
+      CKL();
+      c->launches += 1;
+      return;
+    }
+  }
   if (c->fans && c->dim == 3) {
     FanParams F{c->fan_off.p, c->fan_elem_off.p, c->fan_slot.p, c->finc.p, c->finc_start.p, c->fstride};
     const T *Gf;
@@ -159,8 +179,10 @@ PcgResult run_pcg_t(cfem_ctx *c, Vecs<T> &V, T cK, T cM, const T *mcoef, int war
   const int64_t max_launches = (int64_t)h.maxit / c->chunk + 16;
   int last_iter = -1, stalled = 0;
   for (int64_t launch = 0;; ++launch) {
-    if (launch > max_launches || stalled > 4)
+    if (launch > max_launches || stalled > 4) {
+      check_copy_error(c);
       throw Fail{CFEM_ERR_CUDA, "PCG recurrence stopped advancing on the device"};
+    }
     CK(cudaGraphLaunch(gc.exec, c->stream));
     c->launches += 2 * c->chunk;
     CK(cudaMemcpyAsync(c->h_sc, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, c->stream));
@@ -171,6 +193,7 @@ PcgResult run_pcg_t(cfem_ctx *c, Vecs<T> &V, T cK, T cM, const T *mcoef, int war
     stalled = c->h_sc->iter == last_iter ? stalled + 1 : 0;
     last_iter = c->h_sc->iter;
   }
+  check_copy_error(c);
   res.iters = c->h_sc->iter;
   res.gamma0 = c->h_sc->gamma0;
   res.gamma = c->h_sc->gamma;
@@ -238,6 +261,7 @@ void true_residual(cfem_ctx *c, const double *f, const double *x, double *r, flo
   CK(cudaStreamSynchronize(c->stream));
   rr = c->h_rr[0];
   ff = c->h_rr[1];
+  check_copy_error(c);
 }
 
 void set_diag_vectors(cfem_ctx *c, const double *diagA64) {
@@ -421,6 +445,44 @@ void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, co
       for (int32_t e = P.fan_elem_off[f]; e < P.fan_elem_off[f + 1]; ++e) pos[e] = (int32_t)(f * 8 + (e - P.fan_elem_off[f]));
     c->fan_pos.upload(pos.data(), pos.size(), s);
     c->fan_perm.upload(P.fan_perm.data(), P.fan_perm.size(), s);
+    // patch blocks: the non-gradient prefix is built here, the gradients by
+    // k_fan_block_gradients whenever the operator is (re)built
+    std::vector<int32_t> fan_patch(P.n_fans);
+    for (int p = 0; p < P.n_patches; ++p)
+      for (int32_t f = P.p_fan_off[p]; f < P.p_fan_off[p + 1]; ++f) fan_patch[f] = p;
+    c->fan_patch.upload(fan_patch.data(), fan_patch.size(), s);
+    c->L32 = fan_block_layout(P.np_max, sizeof(float));
+    const size_t pre = (size_t)c->L32.g_off;
+    std::vector<unsigned char> hb(pre * P.n_patches, 0);
+    for (int p = 0; p < P.n_patches; ++p) {
+      unsigned char *B = hb.data() + pre * p;
+      uint16_t *sl = reinterpret_cast<uint16_t *>(B + c->L32.slot_off);
+      uint16_t *fp = reinterpret_cast<uint16_t *>(B + c->L32.fpos_off);
+      uint16_t *fst = reinterpret_cast<uint16_t *>(B + c->L32.fstart_off);
+      int32_t *nd = reinterpret_cast<int32_t *>(B + c->L32.nodes_off);
+      uint8_t *bt = B + c->L32.bits_off;
+      const int f0 = P.p_fan_off[p], nf = P.p_fan_off[p + 1] - f0;
+      const int nb = P.p_node_off[p], n = P.p_node_off[p + 1] - nb;
+      for (int fl = 0; fl < nf; ++fl)
+        for (int k = 0; k < kFanSlots; ++k) sl[k * kFanThreads + fl] = P.fan_slot[(size_t)(f0 + fl) * kFanSlots + k];
+      const int total = P.finc_start[nb + p + n];
+      for (int q = 0; q < total; ++q) {
+        const int code = P.finc[(size_t)kFanSlots * f0 + q];
+        fp[(code & 15) * kFanThreads + (code >> 4)] = (uint16_t)q;
+      }
+      for (int i = 0; i < c->L32.nps; ++i) fst[i] = i <= n ? P.finc_start[nb + p + i] : (uint16_t)total;
+      for (int i = 0; i < c->L32.npn; ++i) {
+        nd[i] = i < n ? P.p_nodes[nb + i] : P.p_nodes[nb];
+        bt[i] = i < n ? P.node_bits[P.p_nodes[nb + i]] : 0;
+      }
+    }
+    c->blk32.alloc((size_t)c->L32.bytes * P.n_patches);
+    c->blk32.zero(s);
+    CK(cudaMemcpy2DAsync(c->blk32.p, c->L32.bytes, hb.data(), pre, pre, P.n_patches, cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));  // hb is pageable and goes out of scope
+    c->tma_err.alloc(1);
+    c->tma_err.zero(s);
+    CK(cudaMallocHost(&c->h_tma_err, sizeof(int)));
   }
   c->bits.upload(P.node_bits.data(), P.node_bits.size(), s);
   // coordinates and global connectivity in the new order (setup + checks)
@@ -508,9 +570,19 @@ void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, co
     int occf = 1;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occf, k_matvec_fan<float, MV_PCG>, kFanThreads, c->smem_fan32));
     c->grid_fan = (int)std::min<int64_t>(P.n_patches, (int64_t)c->n_sm * std::max(occf, 1));
+    c->smem_ft32 = fan_tma_smem_bytes(c->L32, sizeof(float));
+    if (c->smem_ft32 + 8192 > (size_t)smem_optin) c->fan_tma = false;
+    if (c->fan_tma) {
+      for (const void *k : {(const void *)k_matvec_fan_tma<float, MV_PLAIN>, (const void *)k_matvec_fan_tma<float, MV_PCG>,
+                            (const void *)k_matvec_fan_tma<float, MV_DYN>})
+        CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin - 8192));
+      int o32 = 1;
+      CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o32, k_matvec_fan_tma<float, MV_PCG>, kFanThreads, c->smem_ft32));
+      c->grid_ft32 = (int)std::min<int64_t>(P.n_patches, (int64_t)c->n_sm * std::max(o32, 1));
+    }
   }
   c->grid_vec = (int)std::min<int64_t>(std::max<int64_t>(1, nblk(c->nn)), (int64_t)c->n_sm * 4);
-  int maxgrid = std::max({c->grid_mv, c->grid_vec, c->grid_fan});
+  int maxgrid = std::max({c->grid_mv, c->grid_vec, c->grid_fan, c->grid_ft32});
   c->partials.alloc((size_t)maxgrid * 4);
   c->counters.alloc(4);
   c->counters.zero(s);
@@ -591,6 +663,9 @@ void rebuild_operator(cfem_ctx *c) {
     k_fan_gradients<<<nblk(c->ne), kThreads, 0, s>>>(c->ne, c->G64.p, c->gstride, c->fan_pos.p, c->fan_perm.p, c->Gf64.p,
                                                      c->Gf32.p, c->fstride);
     CKL();
+    k_fan_block_gradients<<<nblk(c->ne), kThreads, 0, s>>>(c->ne, c->G64.p, c->gstride, c->fan_pos.p, c->fan_perm.p,
+                                                           c->fan_patch.p, c->fan_off.p, c->blk32.p, c->L32);
+    CKL();
   }
   // consistent-mass diagonal: 2 * cons_c * rho * V per DOF, assembled = mlump * 2 cons_c / lump_c
   k_axpby64<<<nblk(c->nvec), kThreads, 0, s>>>(c->nvec, 2 * cons_c / lump_c, c->mlump.p, 0.0, c->mcdiag.p);
@@ -628,6 +703,16 @@ void attach_stream(cfem_ctx *c, cudaStream_t s) {
     if (!c->ev_in) CK(cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming));
   } else {
     c->stream = s;
+  }
+}
+
+void check_copy_error(cfem_ctx *c) {
+  if (!c->h_tma_err) return;
+  CK(cudaMemcpyAsync(c->h_tma_err, c->tma_err.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (*c->h_tma_err) {
+    c->tma_err.zero(c->stream);
+    throw Fail{CFEM_ERR_CUDA, "a bulk copy of the edge-fan matvec did not complete in time"};
   }
 }
 
@@ -854,7 +939,7 @@ cfem_status cfem_matvec(cfem_ctx *ctx, int32_t precision, const void *x, void *y
     } else {
       throw Fail{CFEM_ERR_INVALID_ARGUMENT, "matvec precision must be CFEM_FP64 or CFEM_FP32"};
     }
-    CK(cudaStreamSynchronize(ctx->stream));
+    check_copy_error(ctx);
     return CFEM_OK;
   });
 }
@@ -940,7 +1025,7 @@ cfem_status cfem_profile_matvec(cfem_ctx *ctx, int32_t precision, int32_t n_laun
       *bytes_per_launch = (double)ctx->ne * (ctx->ncomp * ts + 8) + (double)ctx->nn * ctx->vw * ts * 4;
     // leave the work vectors clean for the next solve
     if (precision == CFEM_FP64) ctx->v64.u.zero(ctx->stream); else ctx->v32.u.zero(ctx->stream);
-    CK(cudaStreamSynchronize(ctx->stream));
+    check_copy_error(ctx);
     return CFEM_OK;
   });
 }

@@ -300,7 +300,7 @@ cfem_status run_dyn(cfem_ctx *c, const cfem_dyn_params *prm, const cfem_wavelet 
   CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
   to_caller<T>(c, dcur, u_out);
   if (nrec) CK(cudaMemcpyAsync(prm->receiver_trace, trace.p, sizeof(double) * trace.n, cudaMemcpyDefault, c->stream));
-  CK(cudaStreamSynchronize(c->stream));
+  check_copy_error(c);
   if (info) {
     info->status = status;
     info->steps = nsteps;
@@ -461,7 +461,7 @@ cfem_status run_dyn_adjoint(cfem_ctx *c, const cfem_dyn_params *prm, const cfem_
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
   if (dLdE) CK(cudaMemcpyAsync(dLdE, gE.p, sizeof(double) * c->ne, cudaMemcpyDefault, c->stream));
-  CK(cudaStreamSynchronize(c->stream));
+  check_copy_error(c);
   if (loss) *loss = L;
   if (info) {
     info->status = CFEM_OK;

@@ -15,6 +15,7 @@
 #include "../../include/cfem.h"
 #include "kernels.cuh"
 #include "kernels_fan.cuh"
+#include "kernels_fan_tma.cuh"
 #include "prep.hpp"
 
 namespace cfem {
@@ -118,6 +119,15 @@ struct cfem_ctx {
   DBuf<float> Gf32;
   size_t smem_fan64 = 0, smem_fan32 = 0;
   int grid_fan = 0;
+  // edge-fan form, FP32, with bulk-copied patch blocks (kernels_fan_tma.cuh)
+  bool fan_tma = true;
+  FanBlockLayout L32{};
+  DBuf<unsigned char> blk32;
+  DBuf<int32_t> fan_patch;
+  DBuf<int> tma_err;
+  int *h_tma_err = nullptr;
+  size_t smem_ft32 = 0;
+  int grid_ft32 = 0;
   int np_slots = 0;               // node slots per patch in shared memory
   DBuf<uint8_t> bits;
   DBuf<double> coords, escale, young_d;
@@ -153,6 +163,7 @@ struct cfem_ctx {
     graph32.reset();
     if (h_sc) cudaFreeHost(h_sc);
     if (h_rr) cudaFreeHost(h_rr);
+    if (h_tma_err) cudaFreeHost(h_tma_err);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (ev_in) cudaEventDestroy(ev_in);
@@ -187,6 +198,8 @@ void true_residual(cfem_ctx *c, const double *f, const double *x, double *r, flo
 void make_rhs(cfem_ctx *c, double a, double b, double *dst);
 cfem_status run_guarded(const std::function<cfem_status()> &fn);
 void check_ctx(const cfem_ctx *c);
+// Throws if a bulk-copy wait of the edge-fan matvec timed out (synchronises the stream).
+void check_copy_error(cfem_ctx *c);
 // Orders the context's stream after the caller's stream (device inputs written there).
 void enter(cfem_ctx *c);
 cfem_solve_params default_params();

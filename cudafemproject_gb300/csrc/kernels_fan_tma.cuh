@@ -1,0 +1,281 @@
+// Edge-fan EbE matvec with the per-patch data streamed by bulk asynchronous
+// copies. Everything a patch needs apart from the node vectors lives in one
+// contiguous, 128-byte aligned block of the "patch block" array:
+//   [slot: kFanSlots x kFanThreads u16]  patch-local nodes P, Q, R_0.. of each fan, then its length
+//   [fpos: (kFanMax+3) x kFanThreads u16] position of each (fan, slot) force in the node-sorted list
+//   [fstart: nps u16]                     node i sums forces fstart[i] .. fstart[i+1]-1
+//   [nodes: npn i32] [bits: npn u8]       global node ids and constraint bits of the patch nodes
+//   [G: 9 kFanMax x kFanThreads T]        scaled gradients in fan vertex order, row (j*9 + (b-1)*3 + d)
+// One copy per patch, issued two patches ahead into a double buffer, so the
+// operator stream overlaps the arithmetic of the current patch. The forces of
+// a patch are written into the G region of its own buffer once every thread
+// has read its gradients, and the node sums read them back contiguously.
+#pragma once
+
+#include "kernels.cuh"
+#include "prep.hpp"
+#include "tma.cuh"
+
+namespace cfem {
+
+struct FanBlockLayout {
+  int bytes;        // per patch, multiple of 128
+  int slot_off, fpos_off, fstart_off, nodes_off, bits_off, g_off;
+  int nps, npn;     // fstart entries, node entries per patch
+};
+
+inline FanBlockLayout fan_block_layout(int np_max, size_t tsize) {
+  FanBlockLayout L{};
+  auto up = [](int x, int a) { return (x + a - 1) / a * a; };
+  L.nps = up(np_max + 1, 8);
+  L.npn = up(np_max, 4);
+  int off = 0;
+  L.slot_off = off; off += kFanSlots * kFanThreads * 2;
+  L.fpos_off = off; off += (kFanMax + 3) * kFanThreads * 2;
+  L.fstart_off = off; off += L.nps * 2;
+  L.nodes_off = off; off += L.npn * 4;
+  L.bits_off = off; off += up(L.npn, 16);
+  L.g_off = up(off, 128);
+  L.bytes = up(L.g_off + (int)(kFanMax * 9 * kFanThreads * tsize), 128);
+  return L;
+}
+
+inline size_t fan_tma_smem_bytes(const FanBlockLayout &L, size_t tsize) {
+  return (size_t)2 * L.bytes + (size_t)L.npn * 4 * tsize + 16;
+}
+
+struct FanTmaParams {
+  const unsigned char *blocks;  // [n_patches][L.bytes]
+  FanBlockLayout L;
+  const int32_t *fan_off;       // [n_patches + 1]
+  const int32_t *fan_elem_off;  // [n_fans + 1] (consistent-mass coefficients)
+  int *err;                     // kErrTmaTimeout on a copy that never completed
+};
+
+template <typename T, int MODE>
+__global__ void __launch_bounds__(kFanThreads) k_matvec_fan_tma(MvParams<T> P, FanTmaParams F) {
+  constexpr int DIM = 3, VW = 4, NS = kFanMax + 3;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const FanBlockLayout &L = F.L;
+  unsigned char *buf0 = smem_raw, *buf1 = smem_raw + L.bytes;
+  T *sp = reinterpret_cast<T *>(smem_raw + 2 * (size_t)L.bytes);  // [npn][4] staged node values
+  uint64_t *bar = reinterpret_cast<uint64_t *>(sp + (size_t)L.npn * VW);
+  if (MODE == MV_PCG && P.sc->done) return;
+  T beta = 0;
+  if (MODE == MV_PCG) beta = P.sc->iter == 0 ? T(0) : T(P.sc->gamma / P.sc->gamma_prev);
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  const int step = gridDim.x;
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < 2; ++k) {
+      const int q = blockIdx.x + k * step;
+      if (q < P.n_patches) {
+        mbar_expect_tx(&bar[k], (unsigned)L.bytes);
+        bulk_load(k ? buf1 : buf0, F.blocks + (size_t)q * L.bytes, (unsigned)L.bytes, &bar[k]);
+      }
+    }
+  }
+  double energy = 0;
+  int it = 0;
+  for (int patch = blockIdx.x; patch < P.n_patches; patch += step, ++it) {
+    const int b = it & 1;
+    unsigned char *B = b ? buf1 : buf0;
+    const bool ok = mbar_wait_bounded(&bar[b], (unsigned)((it >> 1) & 1));
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) {
+        atomicOr(F.err, kErrTmaTimeout);
+        if (patch + step < P.n_patches) mbar_wait_bounded(&bar[b ^ 1], (unsigned)(((it + 1) >> 1) & 1));
+      }
+      return;
+    }
+    const uint16_t *sl = reinterpret_cast<const uint16_t *>(B + L.slot_off);
+    const uint16_t *fpos = reinterpret_cast<const uint16_t *>(B + L.fpos_off);
+    const uint16_t *fstart = reinterpret_cast<const uint16_t *>(B + L.fstart_off);
+    const int32_t *nodes = reinterpret_cast<const int32_t *>(B + L.nodes_off);
+    const uint8_t *bits = B + L.bits_off;
+    const T *Gs = reinterpret_cast<const T *>(B + L.g_off);
+    const int nn = P.node_off[patch + 1] - P.node_off[patch], own = P.own[patch];
+    const int nf = F.fan_off[patch + 1] - F.fan_off[patch];
+    // 1. stage node values
+    for (int i = threadIdx.x; i < nn; i += blockDim.x) {
+      const int g = nodes[i];
+      NodeV<T, VW> v = ldv<T, VW>(P.x, g);
+      if (MODE == MV_PCG) {
+        if (beta != T(0)) {
+          NodeV<T, VW> po = ldv<T, VW>(P.x2, g);
+#pragma unroll
+          for (int d = 0; d < DIM; ++d) v.v[d] += beta * po.v[d];
+        }
+        if (i >= own) stv<T, VW>(P.xout, g, v);
+      } else if (MODE == MV_DYN) {
+        NodeV<T, VW> vv = ldv<T, VW>(P.x2, g), aa = ldv<T, VW>(P.x3, g);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) v.v[d] += P.c1 * vv.v[d] + P.c2 * aa.v[d];
+        if (i >= own) stv<T, VW>(P.xout, g, v);
+      }
+      const unsigned bb = bits[i];
+      NodeV<T, VW> m;
+#pragma unroll
+      for (int d = 0; d < VW; ++d) m.v[d] = (d < DIM && !(bb >> d & 1u)) ? v.v[d] : T(0);
+      stv<T, VW>(sp, i, m);
+    }
+    __syncthreads();
+    // 2. one fan per thread, forces kept in registers
+    const int fl = threadIdx.x;
+    const int len = fl < nf ? sl[(kFanSlots - 1) * kFanThreads + fl] : 0;
+    const int nslot = fl < nf ? len + 3 : 0;  // node slots of this thread's fan (none past the patch's fans)
+    T fv[NS][DIM];
+    {
+      T uv[NS][DIM];
+#pragma unroll
+      for (int k = 0; k < NS; ++k) {
+        NodeV<T, VW> s;
+#pragma unroll
+        for (int d = 0; d < VW; ++d) s.v[d] = 0;
+        if (k < nslot) s = ldv<T, VW>(sp, sl[k * kFanThreads + fl]);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+          uv[k][d] = s.v[d];
+          fv[k][d] = 0;
+        }
+      }
+      const int64_t fe0 = (P.mcoef && fl < nf) ? F.fan_elem_off[F.fan_off[patch] + fl] : 0;
+      T e_fan = 0;
+#pragma unroll
+      for (int j = 0; j < kFanMax; ++j) {
+        if (j < len) {
+          T G[9];
+#pragma unroll
+          for (int k = 0; k < 9; ++k) G[k] = Gs[(j * 9 + k) * kFanThreads + fl];
+          T u[4][DIM], fe[4][DIM];
+#pragma unroll
+          for (int d = 0; d < DIM; ++d) {
+            u[0][d] = uv[0][d];
+            u[1][d] = uv[1][d];
+            u[2][d] = uv[2 + j][d];
+            u[3][d] = uv[3 + j][d];
+          }
+          const T mc = P.mcoef ? P.cM * P.mcoef[fe0 + j] : T(0);
+          element_force<T, DIM>(u, G, P.lam, P.mu, P.cK, mc, fe);
+#pragma unroll
+          for (int d = 0; d < DIM; ++d) {
+            if (MODE == MV_PCG) e_fan += u[0][d] * fe[0][d] + u[1][d] * fe[1][d] + u[2][d] * fe[2][d] + u[3][d] * fe[3][d];
+            fv[0][d] += fe[0][d];
+            fv[1][d] += fe[1][d];
+            fv[2 + j][d] += fe[2][d];
+            fv[3 + j][d] += fe[3][d];
+          }
+        }
+      }
+      if (MODE == MV_PCG) energy += (double)e_fan;
+    }
+    __syncthreads();  // every thread has read its gradients: the G region becomes the force list
+    T *fs = reinterpret_cast<T *>(B + L.g_off);
+#pragma unroll
+    for (int k = 0; k < NS; ++k)
+      if (k < nslot) {
+        NodeV<T, VW> o;
+#pragma unroll
+        for (int d = 0; d < VW; ++d) o.v[d] = d < DIM ? fv[k][d] : T(0);
+        stv<T, VW>(fs, fpos[k * kFanThreads + fl], o);
+      }
+    __syncthreads();
+    // 3. node sums over contiguous force runs
+    for (int i = threadIdx.x; i < nn; i += blockDim.x) {
+      const int g = nodes[i];
+      const unsigned bb = bits[i];
+      T acc[DIM] = {0, 0, 0};
+      const int k1 = fstart[i + 1];
+      for (int k = fstart[i]; k < k1; ++k) {
+        const NodeV<T, VW> fo = ldv<T, VW>(fs, k);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) acc[d] += fo.v[d];
+      }
+      NodeV<T, VW> r;
+      bool any = false;
+#pragma unroll
+      for (int d = 0; d < VW; ++d) {
+        T val = (d < DIM && !(bb >> d & 1u)) ? acc[d < DIM ? d : 0] : T(0);
+        r.v[d] = val;
+        any |= val != T(0);
+      }
+      if (bb && i >= own) {
+        // (I - P) diag(A) x on the constrained DOFs of an owned node
+        NodeV<T, VW> v = ldv<T, VW>(P.x, g);
+        if (MODE == MV_PCG && beta != T(0)) {
+          NodeV<T, VW> po = ldv<T, VW>(P.x2, g);
+#pragma unroll
+          for (int d = 0; d < DIM; ++d) v.v[d] += beta * po.v[d];
+        } else if (MODE == MV_DYN) {
+          NodeV<T, VW> vv = ldv<T, VW>(P.x2, g), aa = ldv<T, VW>(P.x3, g);
+#pragma unroll
+          for (int d = 0; d < DIM; ++d) v.v[d] += P.c1 * vv.v[d] + P.c2 * aa.v[d];
+        }
+        NodeV<T, VW> dg = ldv<T, VW>(P.diagA, g);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d)
+          if (bb >> d & 1u) {
+            T t = dg.v[d] * v.v[d];
+            r.v[d] = t;
+            any |= t != T(0);
+            if (MODE == MV_PCG) energy += (double)(t * v.v[d]);
+          }
+      }
+      if (any) atomic_addv<T, VW>(P.y, g, r, DIM);
+    }
+    // Buffer b is free again. Every thread orders its own generic-proxy
+    // accesses of it (the force stores and reads) before the bulk copy that
+    // refills it, then the barrier makes that true for all of them.
+    fence_proxy_async();
+    __syncthreads();
+    if (threadIdx.x == 0 && patch + 2 * step < P.n_patches) {
+      mbar_expect_tx(&bar[b], (unsigned)L.bytes);
+      bulk_load(B, F.blocks + (size_t)(patch + 2 * step) * L.bytes, (unsigned)L.bytes, &bar[b]);
+    }
+  }
+  if (MODE == MV_PCG) {
+    double v[1] = {energy};
+    if (grid_sum_last<1>(v, P.partials, &P.sc->count_mv)) P.sc->sigma = v[0];
+  }
+}
+
+// Scaled gradients into the G part of the FP32 patch blocks from the
+// element-order FP64 gradients, in fan vertex order.
+static __global__ void k_fan_block_gradients(int64_t ne, const double *G64, int64_t gstride, const int32_t *fan_pos,
+                                             const uint8_t *fan_perm, const int32_t *fan_patch, const int32_t *fan_off,
+                                             unsigned char *blk32, FanBlockLayout L32) {
+  int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  double g[4][3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    double s0 = 0;
+#pragma unroll
+    for (int a = 1; a < 4; ++a) {
+      g[a][d] = G64[(size_t)((a - 1) * 3 + d) * gstride + e];
+      s0 += g[a][d];
+    }
+    g[0][d] = -s0;
+  }
+  const int fp = fan_pos[e];
+  const int f = fp >> 3, j = fp & 7;
+  const int p = fan_patch[f];
+  const int fl = f - fan_off[p];
+  float *G32b = reinterpret_cast<float *>(blk32 + (size_t)p * L32.bytes + L32.g_off);
+  const unsigned perm = fan_perm[e];
+#pragma unroll
+  for (int b = 1; b < 4; ++b) {
+    const int a = (perm >> (2 * b)) & 3u;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const int row = j * 9 + (b - 1) * 3 + d;
+      G32b[row * kFanThreads + fl] = (float)g[a][d];
+    }
+  }
+}
+
+}  // namespace cfem

@@ -181,6 +181,23 @@ def test_jittered_box_patch_sizes(form):
 
 
 @pytest.mark.parametrize("form", ["gradient", "fan"])
+def test_many_patches_per_cta(form):
+    """56k tets in patches of at most 64: every CTA walks several patches, so
+    the double-buffered patch stream reuses each buffer several times."""
+    from cudafemproject_gb300.solver import FemContext
+    p = meshgen.box_3d(14, 14, 48, jitter=0.2, seed=5, traction=(0.0, -1e3, 0.0))
+    o = O.Oracle(p)
+    ctx = FemContext(p, patch_elems=64, matvec_form=form)
+    assert ctx.counts()["n_patches"] > 3 * 152
+    rng = np.random.default_rng(4)
+    for _ in range(2):
+        x = rng.standard_normal(p.n_dof)
+        assert rel(ctx.matvec(x, "fp64"), o.matvec(x)) < 1e-12  # FP64 rounding, 56k tets
+        y32 = ctx.matvec(x.astype(np.float32), "fp32")
+        assert rel(y32, o.matvec(x.astype(np.float32).astype(np.float64))) < 2e-6
+
+
+@pytest.mark.parametrize("form", ["gradient", "fan"])
 @pytest.mark.parametrize("pe", [96, 768])
 def test_unstructured_tets_both_forms(form, pe):
     """Delaunay mesh of random points: edge fans of every length 1..6, open and
