@@ -120,12 +120,36 @@ __device__ __forceinline__ void block_sum(double (&v)[N]) {
   __syncthreads();
 }
 
-// Publishes this block's partial sums; returns true in thread 0 of the last
-// block to finish, which then holds the grid totals (summed in block order, so
-// the result does not depend on scheduling).
+// Sum of the per-block partials in the last block: strided per-thread sums,
+// a shuffle tree per warp and the warp totals in warp order, so the result is
+// a fixed function of the partials. Result valid in thread 0.
 template <int N>
-__device__ __forceinline__ bool grid_sum_last(double (&v)[N], double *partials, unsigned int *count) {
-  block_sum<N>(v);
+__device__ __forceinline__ void last_block_total(double (&v)[N], const double *partials) {
+  __shared__ double red2[N][kThreads / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    double s = 0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) s += __ldcg(partials + (size_t)b * N + k);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) red2[k][wid] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      double t = 0;
+      for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += red2[k][i];
+      v[k] = t;
+    }
+  }
+}
+
+// Publishes this block's partial sums (thread 0 holds them after block_sum);
+// returns true in thread 0 of the last block to finish, which then holds the
+// grid totals. The ticket counter is reset for the next launch.
+template <int N>
+__device__ __forceinline__ bool publish_and_total(double (&v)[N], double *partials, unsigned int *count) {
   __shared__ bool last;
   if (threadIdx.x == 0) {
 #pragma unroll
@@ -137,28 +161,83 @@ __device__ __forceinline__ bool grid_sum_last(double (&v)[N], double *partials, 
   __syncthreads();
   if (!last) return false;
   __threadfence();
-  // every block's partials are visible; sum them in block order
-  double s[N];
-#pragma unroll
-  for (int k = 0; k < N; ++k) s[k] = 0;
-  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
-#pragma unroll
-    for (int k = 0; k < N; ++k) s[k] += __ldcg(partials + (size_t)b * N + k);
-  // fixed-order block reduction of the strided sums
-  __shared__ double red2[N][kThreads];
-#pragma unroll
-  for (int k = 0; k < N; ++k) red2[k][threadIdx.x] = s[k];
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int k = 0; k < N; ++k) {
-      double t = 0;
-      for (int i = 0; i < (int)blockDim.x; ++i) t += red2[k][i];
-      v[k] = t;
-    }
-    *count = 0;
-  }
+  last_block_total<N>(v, partials);
+  if (threadIdx.x == 0) *count = 0;
   return threadIdx.x == 0;
 }
+
+// Grid sum of N doubles per thread (block order, scheduling-independent).
+template <int N>
+__device__ __forceinline__ bool grid_sum_last(double (&v)[N], double *partials, unsigned int *count) {
+  block_sum<N>(v);
+  return publish_and_total<N>(v, partials, count);
+}
+
+// ---- compensated FP32 accumulation ------------------------------------------
+// GB300's FP64 pipe is narrow, so the FP32 kernels accumulate their dot
+// products as unevaluated float pairs (hi + lo, Knuth's TwoSum) per thread and
+// per warp, and switch to FP64 only for the warp totals, the block and the
+// grid sums. The pair carries about 48 significant bits.
+struct Comp32 {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float v) {
+    const float s = hi + v, bp = s - hi;
+    lo += (hi - (s - bp)) + (v - bp);
+    hi = s;
+  }
+  __device__ __forceinline__ void merge(float h2, float l2) {
+    const float s = hi + h2, bp = s - hi;
+    lo = lo + l2 + ((hi - (s - bp)) + (h2 - bp));
+    hi = s;
+  }
+};
+
+// Per-thread accumulator in the working precision's reduction type.
+template <typename T>
+struct DotAcc {
+  double s = 0;
+  __device__ __forceinline__ void add(double v) { s += v; }
+};
+template <>
+struct DotAcc<float> {
+  Comp32 c;
+  __device__ __forceinline__ void add(float v) { c.add(v); }
+};
+
+// Grid sum of N accumulators per thread; true in thread 0 of the last block,
+// whose v then holds the totals.
+template <int N, typename T>
+__device__ __forceinline__ bool grid_sum_acc(DotAcc<T> (&a)[N], double (&v)[N], double *partials, unsigned int *count) {
+  if constexpr (sizeof(T) == 8) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) v[k] = a[k].s;
+    return grid_sum_last<N>(v, partials, count);
+  } else {
+    __shared__ double red[N][kThreads / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      Comp32 c = a[k].c;
+      for (int o = 16; o > 0; o >>= 1) {
+        const float h2 = __shfl_down_sync(0xffffffffu, c.hi, o), l2 = __shfl_down_sync(0xffffffffu, c.lo, o);
+        c.merge(h2, l2);
+      }
+      if (lane == 0) red[k][wid] = (double)c.hi + (double)c.lo;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+      for (int k = 0; k < N; ++k) {
+        double s = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += red[k][i];
+        v[k] = s;
+      }
+    }
+    __syncthreads();
+    return publish_and_total<N>(v, partials, count);
+  }
+}
+
 
 // ------------------------------------------------------------------ element kernel
 // Stiffness (and consistent mass) action of one element in gradient form.
@@ -259,7 +338,7 @@ __global__ void __launch_bounds__(kThreads) k_matvec(MvParams<T> P) {
   if (MODE == MV_PCG && P.sc->done) return;
   T beta = 0;
   if (MODE == MV_PCG) beta = P.sc->iter == 0 ? T(0) : T(P.sc->gamma / P.sc->gamma_prev);
-  double energy = 0;
+  DotAcc<T> energy;
   for (int patch = blockIdx.x; patch < P.n_patches; patch += gridDim.x) {
     const int nb = P.node_off[patch], nn = P.node_off[patch + 1] - nb, own = P.own[patch];
     const int e0 = P.elem_off[patch], ne = P.elem_off[patch + 1] - e0;
@@ -324,7 +403,7 @@ __global__ void __launch_bounds__(kThreads) k_matvec(MvParams<T> P) {
           if (MODE == MV_PCG) e_elem += u[a][d] * f[a][d];
         stv<T, VW>(fs, (size_t)a * P.pe + le, o);
       }
-      if (MODE == MV_PCG) energy += (double)e_elem;
+      if (MODE == MV_PCG) energy.add(e_elem);
     }
     __syncthreads();
     // 3. nodes
@@ -368,7 +447,7 @@ __global__ void __launch_bounds__(kThreads) k_matvec(MvParams<T> P) {
             T t = dg.v[d] * v.v[d];
             r.v[d] = t;
             any |= t != T(0);
-            if (MODE == MV_PCG) energy += (double)(t * v.v[d]);
+            if (MODE == MV_PCG) energy.add(t * v.v[d]);
           }
       }
       if (any) atomic_addv<T, VW>(P.y, g, r, DIM);
@@ -376,8 +455,9 @@ __global__ void __launch_bounds__(kThreads) k_matvec(MvParams<T> P) {
     __syncthreads();
   }
   if (MODE == MV_PCG) {
-    double v[1] = {energy};
-    if (grid_sum_last<1>(v, P.partials, &P.sc->count_mv)) P.sc->sigma = v[0];
+    DotAcc<T> ea[1] = {energy};
+    double v[1];
+    if (grid_sum_acc<1, T>(ea, v, P.partials, &P.sc->count_mv)) P.sc->sigma = v[0];
   }
 }
 
@@ -403,7 +483,7 @@ struct VecParams {
 template <typename T, int DIM>
 __global__ void __launch_bounds__(kThreads) k_pcg_init(VecParams<T> P, int warm) {
   constexpr int VW = DIM == 3 ? 4 : 2;
-  double acc[3] = {0, 0, 0};  // r.z, r.r, f.f
+  DotAcc<T> acc[3];  // r.z, r.r, f.f
   for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < P.n_nodes; n += (int64_t)gridDim.x * blockDim.x) {
     NodeV<T, VW> f = ldv<T, VW>(P.f, n), di = ldv<T, VW>(P.dinv, n), r, z, zero;
     NodeV<T, VW> u = ldv<T, VW>(P.u, n);
@@ -418,15 +498,17 @@ __global__ void __launch_bounds__(kThreads) k_pcg_init(VecParams<T> P, int warm)
       rr += r.v[d] * r.v[d];
       ff += f.v[d] * f.v[d];
     }
-    acc[0] += (double)rz;
-    acc[1] += (double)rr;
-    acc[2] += (double)ff;
+    acc[0].add(rz);
+    acc[1].add(rr);
+    acc[2].add(ff);
     stv<T, VW>(P.r, n, r);
     stv<T, VW>(P.z, n, z);
     stv<T, VW>(P.u, n, zero);
     if (!warm) stv<T, VW>(P.x, n, zero);
   }
-  if (grid_sum_last<3>(acc, P.partials, &P.sc->count_up)) {
+  double tot[3];
+  if (grid_sum_acc<3, T>(acc, tot, P.partials, &P.sc->count_up)) {
+    const double *acc = tot;
     Scalars *s = P.sc;
     s->gamma0 = s->gamma = s->gamma_prev = acc[0];
     s->rr = acc[1];
@@ -449,7 +531,7 @@ __global__ void __launch_bounds__(kThreads) k_pcg_update(VecParams<T> P) {
   if (s->done) return;
   const double alpha_d = s->gamma / s->sigma;
   const T alpha = (T)alpha_d;
-  double acc[2] = {0, 0};
+  DotAcc<T> acc[2];
   for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < P.n_nodes; n += (int64_t)gridDim.x * blockDim.x) {
     NodeV<T, VW> x = ldv<T, VW>(P.x, n), r = ldv<T, VW>(P.r, n), p = ldv<T, VW>(P.p, n), u = ldv<T, VW>(P.u, n);
     NodeV<T, VW> di = ldv<T, VW>(P.dinv, n), z, zero;
@@ -464,14 +546,16 @@ __global__ void __launch_bounds__(kThreads) k_pcg_update(VecParams<T> P) {
       rz += r.v[d] * z.v[d];
       rr += r.v[d] * r.v[d];
     }
-    acc[0] += (double)rz;
-    acc[1] += (double)rr;
+    acc[0].add(rz);
+    acc[1].add(rr);
     stv<T, VW>(P.x, n, x);
     stv<T, VW>(P.r, n, r);
     stv<T, VW>(P.z, n, z);
     stv<T, VW>(P.u, n, zero);
   }
-  if (grid_sum_last<2>(acc, P.partials, &s->count_up)) {
+  double tot[2];
+  if (grid_sum_acc<2, T>(acc, tot, P.partials, &s->count_up)) {
+    const double *acc = tot;
     s->gamma_prev = s->gamma;
     s->gamma = acc[0];
     s->rr = acc[1];

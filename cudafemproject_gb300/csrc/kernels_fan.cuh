@@ -43,7 +43,7 @@ __global__ void __launch_bounds__(kFanThreads) k_matvec_fan(MvParams<T> P, FanPa
   if (MODE == MV_PCG && P.sc->done) return;
   T beta = 0;
   if (MODE == MV_PCG) beta = P.sc->iter == 0 ? T(0) : T(P.sc->gamma / P.sc->gamma_prev);
-  double energy = 0;
+  DotAcc<T> energy;
   for (int patch = blockIdx.x; patch < P.n_patches; patch += gridDim.x) {
     const int nb = P.node_off[patch], nn = P.node_off[patch + 1] - nb, own = P.own[patch];
     const int f0 = F.fan_off[patch], nf = F.fan_off[patch + 1] - f0;
@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(kFanThreads) k_matvec_fan(MvParams<T> P, FanPa
           for (int d = 0; d < VW; ++d) o.v[d] = d < DIM ? fv[k][d] : T(0);
           stv<T, VW>(fs, (size_t)k * kFanThreads + fl, o);
         }
-      if (MODE == MV_PCG) energy += (double)e_fan;
+      if (MODE == MV_PCG) energy.add(e_fan);
     }
     __syncthreads();
     // 3. nodes
@@ -173,7 +173,7 @@ __global__ void __launch_bounds__(kFanThreads) k_matvec_fan(MvParams<T> P, FanPa
             T t = dg.v[d] * v.v[d];
             r.v[d] = t;
             any |= t != T(0);
-            if (MODE == MV_PCG) energy += (double)(t * v.v[d]);
+            if (MODE == MV_PCG) energy.add(t * v.v[d]);
           }
       }
       if (any) atomic_addv<T, VW>(P.y, g, r, DIM);
@@ -181,8 +181,9 @@ __global__ void __launch_bounds__(kFanThreads) k_matvec_fan(MvParams<T> P, FanPa
     __syncthreads();
   }
   if (MODE == MV_PCG) {
-    double v[1] = {energy};
-    if (grid_sum_last<1>(v, P.partials, &P.sc->count_mv)) P.sc->sigma = v[0];
+    DotAcc<T> ea[1] = {energy};
+    double v[1];
+    if (grid_sum_acc<1, T>(ea, v, P.partials, &P.sc->count_mv)) P.sc->sigma = v[0];
   }
 }
 

@@ -18,6 +18,8 @@
 
 namespace cfem {
 
+constexpr int kStageUnroll = 3;  // node gathers in flight per thread while staging a patch
+
 struct FanBlockLayout {
   int bytes;        // per patch, multiple of 128
   int slot_off, fpos_off, fstart_off, nodes_off, bits_off, g_off;
@@ -79,7 +81,7 @@ __global__ void __launch_bounds__(kFanThreads) k_matvec_fan_tma(MvParams<T> P, F
       }
     }
   }
-  double energy = 0;
+  DotAcc<T> energy;
   int it = 0;
   for (int patch = blockIdx.x; patch < P.n_patches; patch += step, ++it) {
     const int b = it & 1;
@@ -100,28 +102,43 @@ __global__ void __launch_bounds__(kFanThreads) k_matvec_fan_tma(MvParams<T> P, F
     const T *Gs = reinterpret_cast<const T *>(B + L.g_off);
     const int nn = P.node_off[patch + 1] - P.node_off[patch], own = P.own[patch];
     const int nf = F.fan_off[patch + 1] - F.fan_off[patch];
-    // 1. stage node values
-    for (int i = threadIdx.x; i < nn; i += blockDim.x) {
-      const int g = nodes[i];
-      NodeV<T, VW> v = ldv<T, VW>(P.x, g);
-      if (MODE == MV_PCG) {
-        if (beta != T(0)) {
-          NodeV<T, VW> po = ldv<T, VW>(P.x2, g);
+    // 1. stage node values: each thread issues the gathers of all its nodes
+    //    (up to kStageUnroll) before using any of them
+    constexpr int SU = kStageUnroll;
+    for (int i0 = threadIdx.x; i0 < nn; i0 += SU * kFanThreads) {
+      NodeV<T, VW> v[SU], w[SU], a3[SU];
+      int gi[SU];
 #pragma unroll
-          for (int d = 0; d < DIM; ++d) v.v[d] += beta * po.v[d];
+      for (int q = 0; q < SU; ++q) {
+        const int i = i0 + q * kFanThreads;
+        gi[q] = i < nn ? nodes[i] : -1;
+        if (gi[q] >= 0) {
+          v[q] = ldv<T, VW>(P.x, gi[q]);
+          if ((MODE == MV_PCG && beta != T(0)) || MODE == MV_DYN) w[q] = ldv<T, VW>(P.x2, gi[q]);
+          if (MODE == MV_DYN) a3[q] = ldv<T, VW>(P.x3, gi[q]);
         }
-        if (i >= own) stv<T, VW>(P.xout, g, v);
-      } else if (MODE == MV_DYN) {
-        NodeV<T, VW> vv = ldv<T, VW>(P.x2, g), aa = ldv<T, VW>(P.x3, g);
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) v.v[d] += P.c1 * vv.v[d] + P.c2 * aa.v[d];
-        if (i >= own) stv<T, VW>(P.xout, g, v);
       }
-      const unsigned bb = bits[i];
-      NodeV<T, VW> m;
 #pragma unroll
-      for (int d = 0; d < VW; ++d) m.v[d] = (d < DIM && !(bb >> d & 1u)) ? v.v[d] : T(0);
-      stv<T, VW>(sp, i, m);
+      for (int q = 0; q < SU; ++q) {
+        const int i = i0 + q * kFanThreads;
+        if (gi[q] < 0) continue;
+        if (MODE == MV_PCG) {
+          if (beta != T(0)) {
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) v[q].v[d] += beta * w[q].v[d];
+          }
+          if (i >= own) stv<T, VW>(P.xout, gi[q], v[q]);
+        } else if (MODE == MV_DYN) {
+#pragma unroll
+          for (int d = 0; d < DIM; ++d) v[q].v[d] += P.c1 * w[q].v[d] + P.c2 * a3[q].v[d];
+          if (i >= own) stv<T, VW>(P.xout, gi[q], v[q]);
+        }
+        const unsigned bb = bits[i];
+        NodeV<T, VW> m;
+#pragma unroll
+        for (int d = 0; d < VW; ++d) m.v[d] = (d < DIM && !(bb >> d & 1u)) ? v[q].v[d] : T(0);
+        stv<T, VW>(sp, i, m);
+      }
     }
     __syncthreads();
     // 2. one fan per thread, forces kept in registers
@@ -171,7 +188,7 @@ __global__ void __launch_bounds__(kFanThreads) k_matvec_fan_tma(MvParams<T> P, F
           }
         }
       }
-      if (MODE == MV_PCG) energy += (double)e_fan;
+      if (MODE == MV_PCG) energy.add(e_fan);
     }
     __syncthreads();  // every thread has read its gradients: the G region becomes the force list
     T *fs = reinterpret_cast<T *>(B + L.g_off);
@@ -222,7 +239,7 @@ __global__ void __launch_bounds__(kFanThreads) k_matvec_fan_tma(MvParams<T> P, F
             T t = dg.v[d] * v.v[d];
             r.v[d] = t;
             any |= t != T(0);
-            if (MODE == MV_PCG) energy += (double)(t * v.v[d]);
+            if (MODE == MV_PCG) energy.add(t * v.v[d]);
           }
       }
       if (any) atomic_addv<T, VW>(P.y, g, r, DIM);
@@ -238,8 +255,9 @@ __global__ void __launch_bounds__(kFanThreads) k_matvec_fan_tma(MvParams<T> P, F
     }
   }
   if (MODE == MV_PCG) {
-    double v[1] = {energy};
-    if (grid_sum_last<1>(v, P.partials, &P.sc->count_mv)) P.sc->sigma = v[0];
+    DotAcc<T> ea[1] = {energy};
+    double v[1];
+    if (grid_sum_acc<1, T>(ea, v, P.partials, &P.sc->count_mv)) P.sc->sigma = v[0];
   }
 }
 
