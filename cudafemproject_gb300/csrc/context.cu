@@ -52,7 +52,7 @@ void launch_mv_t(cfem_ctx *c, int mode, const MvParams<T> &P) {
       F.fan_off = c->fan_off.p;
       F.fan_elem_off = c->fan_elem_off.p;
       F.err = c->tma_err.p;
-      dim3 g(c->grid_ft32), b(kFanThreads);
+      dim3 g(c->grid_ft32), b(kHfanThreads);
       if (mode == MV_PLAIN) k_matvec_fan_tma<float, MV_PLAIN><<<g, b, c->smem_ft32, c->stream>>>(P, F);
       else if (mode == MV_PCG) k_matvec_fan_tma<float, MV_PCG><<<g, b, c->smem_ft32, c->stream>>>(P, F);
       else k_matvec_fan_tma<float, MV_DYN><<<g, b, c->smem_ft32, c->stream>>>(P, F);
@@ -465,12 +465,24 @@ void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, co
       const int nb = P.p_node_off[p], n = P.p_node_off[p + 1] - nb;
       for (int fl = 0; fl < nf; ++fl)
         for (int k = 0; k < kFanSlots; ++k) sl[k * kFanThreads + fl] = P.fan_slot[(size_t)(f0 + fl) * kFanSlots + k];
-      const int total = P.finc_start[nb + p + n];
-      for (int q = 0; q < total; ++q) {
-        const int code = P.finc[(size_t)kFanSlots * f0 + q];
-        fp[(code & 15) * kFanThreads + (code >> 4)] = (uint16_t)q;
+      // half-fan incidences (fan fl, half h, slot hs), counting-sorted by node
+      std::vector<int> cnt(n + 1, 0);
+      for (int fl = 0; fl < nf; ++fl) {
+        const int len = P.fan_slot[(size_t)(f0 + fl) * kFanSlots + kFanSlots - 1];
+        for (int h = 0; h < 2; ++h)
+          for (int hs = 0; hs < half_slot_count(h, len); ++hs)
+            ++cnt[P.fan_slot[(size_t)(f0 + fl) * kFanSlots + half_slot_to_fan(h, hs)] + 1];
       }
-      for (int i = 0; i < c->L32.nps; ++i) fst[i] = i <= n ? P.finc_start[nb + p + i] : (uint16_t)total;
+      for (int i = 0; i < n; ++i) cnt[i + 1] += cnt[i];
+      const int total = cnt[n];
+      for (int i = 0; i < c->L32.nps; ++i) fst[i] = (uint16_t)(i <= n ? cnt[i] : total);
+      for (int fl = 0; fl < nf; ++fl) {
+        const int len = P.fan_slot[(size_t)(f0 + fl) * kFanSlots + kFanSlots - 1];
+        for (int h = 0; h < 2; ++h)
+          for (int hs = 0; hs < half_slot_count(h, len); ++hs)
+            fp[(h * 6 + hs) * kFanThreads + fl] =
+                (uint16_t)cnt[P.fan_slot[(size_t)(f0 + fl) * kFanSlots + half_slot_to_fan(h, hs)]]++;
+      }
       for (int i = 0; i < c->L32.npn; ++i) {
         nd[i] = i < n ? P.p_nodes[nb + i] : P.p_nodes[nb];
         bt[i] = i < n ? P.node_bits[P.p_nodes[nb + i]] : 0;
@@ -577,7 +589,7 @@ void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, co
                             (const void *)k_matvec_fan_tma<float, MV_DYN>})
         CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin - 8192));
       int o32 = 1;
-      CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o32, k_matvec_fan_tma<float, MV_PCG>, kFanThreads, c->smem_ft32));
+      CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o32, k_matvec_fan_tma<float, MV_PCG>, kHfanThreads, c->smem_ft32));
       c->grid_ft32 = (int)std::min<int64_t>(P.n_patches, (int64_t)c->n_sm * std::max(o32, 1));
     }
   }

@@ -1,11 +1,13 @@
 // Edge-fan EbE matvec with the per-patch data streamed by bulk asynchronous
-// copies. Everything a patch needs apart from the node vectors lives in one
+// copies. Two threads share a fan: half h evaluates tets 3h .. 3h+2 and owns
+// the six node slots P, Q, R_3h .. R_3h+3 (kHalfSlots = 12 force slots per fan).
+// Everything a patch needs apart from the node vectors lives in one
 // contiguous, 128-byte aligned block of the "patch block" array:
-//   [slot: kFanSlots x kFanThreads u16]  patch-local nodes P, Q, R_0.. of each fan, then its length
-//   [fpos: (kFanMax+3) x kFanThreads u16] position of each (fan, slot) force in the node-sorted list
-//   [fstart: nps u16]                     node i sums forces fstart[i] .. fstart[i+1]-1
-//   [nodes: npn i32] [bits: npn u8]       global node ids and constraint bits of the patch nodes
-//   [G: 9 kFanMax x kFanThreads T]        scaled gradients in fan vertex order, row (j*9 + (b-1)*3 + d)
+//   [slot: kFanSlots x kFanThreads u16]   patch-local nodes P, Q, R_0.. of each fan, then its length
+//   [fpos: kHalfSlots x kFanThreads u16]  position of each (fan, half slot) force in the node-sorted list
+//   [fstart: nps u16]                      node i sums forces fstart[i] .. fstart[i+1]-1
+//   [nodes: npn i32] [bits: npn u8]        global node ids and constraint bits of the patch nodes
+//   [G: 9 kFanMax x kFanThreads T]         scaled gradients in fan vertex order, row (j*9 + (b-1)*3 + d)
 // One copy per patch, issued two patches ahead into a double buffer, so the
 // operator stream overlaps the arithmetic of the current patch. The forces of
 // a patch are written into the G region of its own buffer once every thread
@@ -18,7 +20,16 @@
 
 namespace cfem {
 
-constexpr int kStageUnroll = 3;  // node gathers in flight per thread while staging a patch
+constexpr int kStageUnroll = 2;      // node gathers in flight per thread while staging a patch
+constexpr int kHalfSlots = 12;       // force slots per fan: 2 halves x (P, Q, 4 ring vertices)
+constexpr int kHfanThreads = 2 * kFanThreads;
+
+// fan slot (0 = P, 1 = Q, 2 + k = R_k) of half h's slot hs
+__host__ __device__ __forceinline__ int half_slot_to_fan(int h, int hs) { return hs < 2 ? hs : hs + 3 * h; }
+// number of valid slots of half h of a fan of length len (0 if the half has no tet)
+__host__ __device__ __forceinline__ int half_slot_count(int h, int len) {
+  return len > 3 * h ? 3 + (len - 3 * h < 3 ? len - 3 * h : 3) : 0;
+}
 
 struct FanBlockLayout {
   int bytes;        // per patch, multiple of 128
@@ -33,7 +44,7 @@ inline FanBlockLayout fan_block_layout(int np_max, size_t tsize) {
   L.npn = up(np_max, 4);
   int off = 0;
   L.slot_off = off; off += kFanSlots * kFanThreads * 2;
-  L.fpos_off = off; off += (kFanMax + 3) * kFanThreads * 2;
+  L.fpos_off = off; off += kHalfSlots * kFanThreads * 2;
   L.fstart_off = off; off += L.nps * 2;
   L.nodes_off = off; off += L.npn * 4;
   L.bits_off = off; off += up(L.npn, 16);
@@ -55,8 +66,8 @@ struct FanTmaParams {
 };
 
 template <typename T, int MODE>
-__global__ void __launch_bounds__(kFanThreads) k_matvec_fan_tma(MvParams<T> P, FanTmaParams F) {
-  constexpr int DIM = 3, VW = 4, NS = kFanMax + 3;
+__global__ void __launch_bounds__(kHfanThreads) k_matvec_fan_tma(MvParams<T> P, FanTmaParams F) {
+  constexpr int DIM = 3, VW = 4;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const FanBlockLayout &L = F.L;
   unsigned char *buf0 = smem_raw, *buf1 = smem_raw + L.bytes;
@@ -105,12 +116,12 @@ __global__ void __launch_bounds__(kFanThreads) k_matvec_fan_tma(MvParams<T> P, F
     // 1. stage node values: each thread issues the gathers of all its nodes
     //    (up to kStageUnroll) before using any of them
     constexpr int SU = kStageUnroll;
-    for (int i0 = threadIdx.x; i0 < nn; i0 += SU * kFanThreads) {
+    for (int i0 = threadIdx.x; i0 < nn; i0 += SU * kHfanThreads) {
       NodeV<T, VW> v[SU], w[SU], a3[SU];
       int gi[SU];
 #pragma unroll
       for (int q = 0; q < SU; ++q) {
-        const int i = i0 + q * kFanThreads;
+        const int i = i0 + q * kHfanThreads;
         gi[q] = i < nn ? nodes[i] : -1;
         if (gi[q] >= 0) {
           v[q] = ldv<T, VW>(P.x, gi[q]);
@@ -120,7 +131,7 @@ __global__ void __launch_bounds__(kFanThreads) k_matvec_fan_tma(MvParams<T> P, F
       }
 #pragma unroll
       for (int q = 0; q < SU; ++q) {
-        const int i = i0 + q * kFanThreads;
+        const int i = i0 + q * kHfanThreads;
         if (gi[q] < 0) continue;
         if (MODE == MV_PCG) {
           if (beta != T(0)) {
@@ -141,30 +152,31 @@ __global__ void __launch_bounds__(kFanThreads) k_matvec_fan_tma(MvParams<T> P, F
       }
     }
     __syncthreads();
-    // 2. one fan per thread, forces kept in registers
-    const int fl = threadIdx.x;
+    // 2. half a fan per thread (tets 3h .. 3h+2), forces kept in registers
+    const int fl = threadIdx.x >> 1, h = threadIdx.x & 1;
     const int len = fl < nf ? sl[(kFanSlots - 1) * kFanThreads + fl] : 0;
-    const int nslot = fl < nf ? len + 3 : 0;  // node slots of this thread's fan (none past the patch's fans)
-    T fv[NS][DIM];
+    const int nk = half_slot_count(h, len);
+    T fv[6][DIM];
     {
-      T uv[NS][DIM];
+      T uv[6][DIM];
 #pragma unroll
-      for (int k = 0; k < NS; ++k) {
+      for (int k = 0; k < 6; ++k) {
         NodeV<T, VW> s;
 #pragma unroll
         for (int d = 0; d < VW; ++d) s.v[d] = 0;
-        if (k < nslot) s = ldv<T, VW>(sp, sl[k * kFanThreads + fl]);
+        if (k < nk) s = ldv<T, VW>(sp, sl[half_slot_to_fan(h, k) * kFanThreads + fl]);
 #pragma unroll
         for (int d = 0; d < DIM; ++d) {
           uv[k][d] = s.v[d];
           fv[k][d] = 0;
         }
       }
-      const int64_t fe0 = (P.mcoef && fl < nf) ? F.fan_elem_off[F.fan_off[patch] + fl] : 0;
+      const int64_t fe0 = (P.mcoef && nk) ? F.fan_elem_off[F.fan_off[patch] + fl] : 0;
       T e_fan = 0;
 #pragma unroll
-      for (int j = 0; j < kFanMax; ++j) {
-        if (j < len) {
+      for (int jj = 0; jj < 3; ++jj) {
+        const int j = 3 * h + jj;
+        if (nk && j < len) {
           T G[9];
 #pragma unroll
           for (int k = 0; k < 9; ++k) G[k] = Gs[(j * 9 + k) * kFanThreads + fl];
@@ -173,8 +185,8 @@ __global__ void __launch_bounds__(kFanThreads) k_matvec_fan_tma(MvParams<T> P, F
           for (int d = 0; d < DIM; ++d) {
             u[0][d] = uv[0][d];
             u[1][d] = uv[1][d];
-            u[2][d] = uv[2 + j][d];
-            u[3][d] = uv[3 + j][d];
+            u[2][d] = uv[2 + jj][d];
+            u[3][d] = uv[3 + jj][d];
           }
           const T mc = P.mcoef ? P.cM * P.mcoef[fe0 + j] : T(0);
           element_force<T, DIM>(u, G, P.lam, P.mu, P.cK, mc, fe);
@@ -183,8 +195,8 @@ __global__ void __launch_bounds__(kFanThreads) k_matvec_fan_tma(MvParams<T> P, F
             if (MODE == MV_PCG) e_fan += u[0][d] * fe[0][d] + u[1][d] * fe[1][d] + u[2][d] * fe[2][d] + u[3][d] * fe[3][d];
             fv[0][d] += fe[0][d];
             fv[1][d] += fe[1][d];
-            fv[2 + j][d] += fe[2][d];
-            fv[3 + j][d] += fe[3][d];
+            fv[2 + jj][d] += fe[2][d];
+            fv[3 + jj][d] += fe[3][d];
           }
         }
       }
@@ -193,16 +205,16 @@ __global__ void __launch_bounds__(kFanThreads) k_matvec_fan_tma(MvParams<T> P, F
     __syncthreads();  // every thread has read its gradients: the G region becomes the force list
     T *fs = reinterpret_cast<T *>(B + L.g_off);
 #pragma unroll
-    for (int k = 0; k < NS; ++k)
-      if (k < nslot) {
+    for (int k = 0; k < 6; ++k)
+      if (k < nk) {
         NodeV<T, VW> o;
 #pragma unroll
         for (int d = 0; d < VW; ++d) o.v[d] = d < DIM ? fv[k][d] : T(0);
-        stv<T, VW>(fs, fpos[k * kFanThreads + fl], o);
+        stv<T, VW>(fs, fpos[(h * 6 + k) * kFanThreads + fl], o);
       }
     __syncthreads();
     // 3. node sums over contiguous force runs
-    for (int i = threadIdx.x; i < nn; i += blockDim.x) {
+    for (int i = threadIdx.x; i < nn; i += kHfanThreads) {
       const int g = nodes[i];
       const unsigned bb = bits[i];
       T acc[DIM] = {0, 0, 0};
