@@ -999,6 +999,7 @@ cfem_status cfem_profile_matvec(cfem_ctx *ctx, int32_t precision, int32_t n_laun
     Scalars h{};
     h.iter = 1;
     h.gamma = h.gamma_prev = 1.0;
+    h.beta = 1.0;
     Scalars *sc = ctx->sc.p + 2;
     CK(cudaMemcpyAsync(sc, &h, sizeof(Scalars), cudaMemcpyHostToDevice, ctx->stream));
     const size_t ts = precision == CFEM_FP64 ? 8 : 4;

@@ -38,6 +38,10 @@ struct Scalars {
   int rule, maxit, iter, done;  // done: 0 running, 1 converged, 2 diverged, 3 iteration cap
   unsigned int count_mv, count_up;
   int pad0, pad1;
+  // alpha = gamma / sigma (set by the matvec's last block), beta = gamma / gamma_prev
+  // (set by the update's last block, 0 before the first direction): computed
+  // once, so no thread divides in FP64
+  double alpha, beta;
 };
 
 struct DynState {
@@ -337,7 +341,7 @@ __global__ void __launch_bounds__(kThreads) k_matvec(MvParams<T> P) {
   uint8_t *sb = reinterpret_cast<uint8_t *>(sg + P.np_max);                    // [np_max] BC bits
   if (MODE == MV_PCG && P.sc->done) return;
   T beta = 0;
-  if (MODE == MV_PCG) beta = P.sc->iter == 0 ? T(0) : T(P.sc->gamma / P.sc->gamma_prev);
+  if (MODE == MV_PCG) beta = T(P.sc->beta);
   DotAcc<T> energy;
   for (int patch = blockIdx.x; patch < P.n_patches; patch += gridDim.x) {
     const int nb = P.node_off[patch], nn = P.node_off[patch + 1] - nb, own = P.own[patch];
@@ -457,7 +461,10 @@ __global__ void __launch_bounds__(kThreads) k_matvec(MvParams<T> P) {
   if (MODE == MV_PCG) {
     DotAcc<T> ea[1] = {energy};
     double v[1];
-    if (grid_sum_acc<1, T>(ea, v, P.partials, &P.sc->count_mv)) P.sc->sigma = v[0];
+    if (grid_sum_acc<1, T>(ea, v, P.partials, &P.sc->count_mv)) {
+      P.sc->sigma = v[0];
+      P.sc->alpha = P.sc->gamma / v[0];
+    }
   }
 }
 
@@ -515,6 +522,8 @@ __global__ void __launch_bounds__(kThreads) k_pcg_init(VecParams<T> P, int warm)
     s->ff = acc[2];
     s->iter = 0;
     s->sigma = 0;
+    s->alpha = 0;
+    s->beta = 0;
     int done = 0;
     if (acc[0] == 0.0) done = 1;
     if (s->rule == 1 && sqrt(acc[1]) <= s->tol * sqrt(acc[2])) done = 1;
@@ -529,7 +538,7 @@ __global__ void __launch_bounds__(kThreads) k_pcg_update(VecParams<T> P) {
   constexpr int VW = DIM == 3 ? 4 : 2;
   Scalars *s = P.sc;
   if (s->done) return;
-  const double alpha_d = s->gamma / s->sigma;
+  const double alpha_d = s->alpha;
   const T alpha = (T)alpha_d;
   DotAcc<T> acc[2];
   for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < P.n_nodes; n += (int64_t)gridDim.x * blockDim.x) {
@@ -558,6 +567,7 @@ __global__ void __launch_bounds__(kThreads) k_pcg_update(VecParams<T> P) {
     const double *acc = tot;
     s->gamma_prev = s->gamma;
     s->gamma = acc[0];
+    s->beta = s->gamma / s->gamma_prev;
     s->rr = acc[1];
     s->iter += 1;
     int done = 0;

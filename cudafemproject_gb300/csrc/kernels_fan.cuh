@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(kFanThreads) k_matvec_fan(MvParams<T> P, FanPa
   uint8_t *sb = reinterpret_cast<uint8_t *>(sg + P.np_max);                            // [np_max]
   if (MODE == MV_PCG && P.sc->done) return;
   T beta = 0;
-  if (MODE == MV_PCG) beta = P.sc->iter == 0 ? T(0) : T(P.sc->gamma / P.sc->gamma_prev);
+  if (MODE == MV_PCG) beta = T(P.sc->beta);
   DotAcc<T> energy;
   for (int patch = blockIdx.x; patch < P.n_patches; patch += gridDim.x) {
     const int nb = P.node_off[patch], nn = P.node_off[patch + 1] - nb, own = P.own[patch];
@@ -183,7 +183,10 @@ __global__ void __launch_bounds__(kFanThreads) k_matvec_fan(MvParams<T> P, FanPa
   if (MODE == MV_PCG) {
     DotAcc<T> ea[1] = {energy};
     double v[1];
-    if (grid_sum_acc<1, T>(ea, v, P.partials, &P.sc->count_mv)) P.sc->sigma = v[0];
+    if (grid_sum_acc<1, T>(ea, v, P.partials, &P.sc->count_mv)) {
+      P.sc->sigma = v[0];
+      P.sc->alpha = P.sc->gamma / v[0];
+    }
   }
 }
 

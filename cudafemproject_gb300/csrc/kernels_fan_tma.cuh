@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(kHfanThreads) k_matvec_fan_tma(MvParams<T> P, 
   uint64_t *bar = reinterpret_cast<uint64_t *>(sp + (size_t)L.npn * VW);
   if (MODE == MV_PCG && P.sc->done) return;
   T beta = 0;
-  if (MODE == MV_PCG) beta = P.sc->iter == 0 ? T(0) : T(P.sc->gamma / P.sc->gamma_prev);
+  if (MODE == MV_PCG) beta = T(P.sc->beta);
   if (threadIdx.x == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
@@ -269,7 +269,10 @@ __global__ void __launch_bounds__(kHfanThreads) k_matvec_fan_tma(MvParams<T> P, 
   if (MODE == MV_PCG) {
     DotAcc<T> ea[1] = {energy};
     double v[1];
-    if (grid_sum_acc<1, T>(ea, v, P.partials, &P.sc->count_mv)) P.sc->sigma = v[0];
+    if (grid_sum_acc<1, T>(ea, v, P.partials, &P.sc->count_mv)) {
+      P.sc->sigma = v[0];
+      P.sc->alpha = P.sc->gamma / v[0];
+    }
   }
 }
 
