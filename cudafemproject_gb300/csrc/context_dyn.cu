@@ -500,27 +500,6 @@ cfem_status cfem_dyn(cfem_ctx *ctx, const cfem_dyn_params *prm, const cfem_wavel
   });
 }
 
-cfem_status cfem_pcg_multi(cfem_ctx *ctx, const cfem_solve_params *prm, int32_t k, const double *F, double *U,
-                           cfem_solve_info *info) {
-  return run_guarded([&]() -> cfem_status {
-    check_ctx(ctx);
-    enter(ctx);
-    if (k <= 0 || !F || !U) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "bad multi-RHS arguments"};
-    cfem_solve_params p = prm ? *prm : default_params();
-    cfem_status worst = CFEM_OK;
-    for (int i = 0; i < k; ++i) {
-      cfem_solve_info inf{};
-      to_internal<double>(ctx, F + (size_t)i * ctx->nd, ctx->v64.f.p);
-      cfem_status st = solve_internal(ctx, &p, &inf);
-      to_caller<double>(ctx, ctx->v64.x.p, U + (size_t)i * ctx->nd);
-      if (info) info[i] = inf;
-      if (st != CFEM_OK && worst == CFEM_OK) worst = st;
-    }
-    CK(cudaStreamSynchronize(ctx->stream));
-    return worst;
-  });
-}
-
 cfem_status cfem_adjoint(cfem_ctx *ctx, const cfem_solve_params *prm, const double *u, const double *dLdu, double *dLdE,
                          double *dLdf, cfem_solve_info *info) {
   return run_guarded([&]() -> cfem_status {

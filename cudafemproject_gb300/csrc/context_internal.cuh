@@ -16,12 +16,16 @@
 #include "kernels.cuh"
 #include "kernels_fan.cuh"
 #include "kernels_fan_tma.cuh"
+#include "kernels_multi.cuh"
 #include "prep.hpp"
 
 namespace cfem {
 namespace detail {
 
 extern thread_local std::string g_last_error;
+
+struct MultiState;                    // multi-RHS work arrays (context_multi.cu)
+void destroy_multi(MultiState *m);
 
 struct Fail {
   cfem_status st;
@@ -150,6 +154,7 @@ struct cfem_ctx {
   int grid_mv = 0, grid_vec = 0;
   size_t smem64 = 0, smem32 = 0;
   int chunk = 16;
+  MultiState *multi = nullptr;
   int64_t launches = 0;  // kernels issued since the counter was last reset
   GraphCache graph64, graph32;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -164,6 +169,7 @@ struct cfem_ctx {
     if (h_sc) cudaFreeHost(h_sc);
     if (h_rr) cudaFreeHost(h_rr);
     if (h_tma_err) cudaFreeHost(h_tma_err);
+    if (multi) destroy_multi(multi);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (ev_in) cudaEventDestroy(ev_in);

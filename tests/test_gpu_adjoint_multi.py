@@ -73,6 +73,31 @@ def test_multi_rhs(precision, tol):
         assert rel(U[i], x) <= tol
 
 
+@pytest.mark.parametrize("form,pe", [("fan", 0), ("fan", 64), ("gradient", 0)])
+def test_multi_rhs_batched(form, pe):
+    """37 load cases (padded to 64) through the batched multi-RHS PCG, one of
+    them zero: every case matches the FP64 oracle and its own single-RHS solve."""
+    from cudafemproject_gb300.solver import FemContext
+    p = meshgen.box_3d(6, 5, 16, jitter=0.2, seed=3)
+    o = O.Oracle(p)
+    rng = np.random.default_rng(11)
+    F = rng.standard_normal((37, p.n_dof)) * 10.0 ** rng.uniform(2, 4, size=(37, 1))
+    F[5] = 0.0
+    ctx = FemContext(p, patch_elems=pe, matvec_form=form)
+    U, infos = ctx.pcg_multi(F, precision="fp32_refine", tol=1e-4, stop_rule="residual", outer_tol=1e-12)
+    assert np.all(U[5] == 0.0)
+    for i in (0, 1, 17, 36):
+        x, _ = o.pcg(F[i], tol=1e-14, rule=1)
+        assert rel(U[i], x) <= 1e-8, i
+        assert infos[i]["status"] == 0 and infos[i]["rel_residual"] < 1e-11
+    u_single, _ = ctx.pcg(F[17], "fp32_refine", tol=1e-4, stop_rule="residual", outer_tol=1e-12)
+    assert rel(U[17], u_single) <= 1e-9
+    U32, inf32 = ctx.pcg_multi(F[:9], precision="fp32", tol=1e-6, stop_rule="residual")
+    for i in (0, 8):
+        x, _ = o.pcg(F[i], tol=1e-14, rule=1)
+        assert rel(U32[i], x) <= 1e-4, i
+
+
 def test_torch_autograd_function():
     torch = pytest.importorskip("torch")
     from cudafemproject_gb300.autograd import static_solve
