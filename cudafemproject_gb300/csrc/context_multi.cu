@@ -120,6 +120,7 @@ void autotune_r(cfem_ctx *c, MultiState &M) {
   }
   configure_r(c, M, best_r);
   M.u.zero(c->stream);
+  if (c->verbose) std::printf("multi-RHS: K=%d cases, R=%d cases per thread, %d CTAs\n", M.K, M.R, M.grid_mv);
 }
 
 MultiState &multi_state(cfem_ctx *c, int K) {

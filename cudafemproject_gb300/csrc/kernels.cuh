@@ -291,6 +291,33 @@ __device__ __forceinline__ void element_force(const T (&u)[DIM + 1][DIM], const 
   }
 }
 
+// Stiffness action of a tet from vertex differences du_a = u_a - u_0 (a = 1..3):
+// forces on vertices 1..3 only (the force on vertex 0 is minus their sum).
+// lam, mu already carry the operator's stiffness factor.
+template <typename T>
+__device__ __forceinline__ void tet_forces_rel(const T (&d1)[3], const T (&d2)[3], const T (&d3)[3], const T (&G)[9],
+                                               T lam, T mu, T (&f1)[3], T (&f2)[3], T (&f3)[3]) {
+  T H[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) H[i][j] = d1[i] * G[j] + d2[i] * G[3 + j] + d3[i] * G[6 + j];
+  const T tr = H[0][0] + H[1][1] + H[2][2];
+  T S[3][3];
+  const T two_mu = mu + mu;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) S[i][i] = two_mu * H[i][i] + lam * tr;
+  S[0][1] = S[1][0] = mu * (H[0][1] + H[1][0]);
+  S[0][2] = S[2][0] = mu * (H[0][2] + H[2][0]);
+  S[1][2] = S[2][1] = mu * (H[1][2] + H[2][1]);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    f1[i] = S[i][0] * G[0] + S[i][1] * G[1] + S[i][2] * G[2];
+    f2[i] = S[i][0] * G[3] + S[i][1] * G[4] + S[i][2] * G[5];
+    f3[i] = S[i][0] * G[6] + S[i][1] * G[7] + S[i][2] * G[8];
+  }
+}
+
 // ------------------------------------------------------------------ matvec
 enum MvMode { MV_PLAIN = 0, MV_PCG = 1, MV_DYN = 2 };
 

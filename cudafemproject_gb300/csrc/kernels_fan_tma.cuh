@@ -66,7 +66,8 @@ struct FanTmaParams {
 };
 
 template <typename T, int MODE>
-__global__ void __launch_bounds__(kHfanThreads) k_matvec_fan_tma(MvParams<T> P, FanTmaParams F) {
+// (3 CTAs per SM: the shared memory of a CTA allows 3, the register bound makes them fit)
+__global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> P, FanTmaParams F) {
   constexpr int DIM = 3, VW = 4;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const FanBlockLayout &L = F.L;
@@ -152,7 +153,9 @@ __global__ void __launch_bounds__(kHfanThreads) k_matvec_fan_tma(MvParams<T> P, 
       }
     }
     __syncthreads();
-    // 2. half a fan per thread (tets 3h .. 3h+2), forces kept in registers
+    // 2. half a fan per thread (tets 3h .. 3h+2), forces kept in registers.
+    //    Missing tets have zero gradients in the block, so the three tets are
+    //    straight-line code; differences to P are formed once per node slot.
     const int fl = threadIdx.x >> 1, h = threadIdx.x & 1;
     const int len = fl < nf ? sl[(kFanSlots - 1) * kFanThreads + fl] : 0;
     const int nk = half_slot_count(h, len);
@@ -171,36 +174,66 @@ __global__ void __launch_bounds__(kHfanThreads) k_matvec_fan_tma(MvParams<T> P, 
           fv[k][d] = 0;
         }
       }
-      const int64_t fe0 = (P.mcoef && nk) ? F.fan_elem_off[F.fan_off[patch] + fl] : 0;
-      T e_fan = 0;
+      if (P.mcoef == nullptr) {
+        const T lamk = P.lam * P.cK, muk = P.mu * P.cK;
+        T du[6][DIM];
 #pragma unroll
-      for (int jj = 0; jj < 3; ++jj) {
-        const int j = 3 * h + jj;
-        if (nk && j < len) {
+        for (int k = 1; k < 6; ++k)
+#pragma unroll
+          for (int d = 0; d < DIM; ++d) du[k][d] = uv[k][d] - uv[0][d];
+#pragma unroll
+        for (int jj = 0; jj < 3; ++jj) {
+          const int j = 3 * h + jj;
           T G[9];
 #pragma unroll
           for (int k = 0; k < 9; ++k) G[k] = Gs[(j * 9 + k) * kFanThreads + fl];
-          T u[4][DIM], fe[4][DIM];
+          T f1[3], f2[3], f3[3];
+          tet_forces_rel<T>(du[1], du[2 + jj], du[3 + jj], G, lamk, muk, f1, f2, f3);
 #pragma unroll
           for (int d = 0; d < DIM; ++d) {
-            u[0][d] = uv[0][d];
-            u[1][d] = uv[1][d];
-            u[2][d] = uv[2 + jj][d];
-            u[3][d] = uv[3 + jj][d];
+            fv[1][d] += f1[d];
+            fv[2 + jj][d] += f2[d];
+            fv[3 + jj][d] += f3[d];
           }
-          const T mc = P.mcoef ? P.cM * P.mcoef[fe0 + j] : T(0);
-          element_force<T, DIM>(u, G, P.lam, P.mu, P.cK, mc, fe);
+        }
 #pragma unroll
-          for (int d = 0; d < DIM; ++d) {
-            if (MODE == MV_PCG) e_fan += u[0][d] * fe[0][d] + u[1][d] * fe[1][d] + u[2][d] * fe[2][d] + u[3][d] * fe[3][d];
-            fv[0][d] += fe[0][d];
-            fv[1][d] += fe[1][d];
-            fv[2 + jj][d] += fe[2][d];
-            fv[3 + jj][d] += fe[3][d];
+        for (int d = 0; d < DIM; ++d) fv[0][d] = -(fv[1][d] + fv[2][d] + fv[3][d] + fv[4][d] + fv[5][d]);
+      } else {  // consistent mass term: forces do not sum to zero per tet
+        const int64_t fe0 = nk ? F.fan_elem_off[F.fan_off[patch] + fl] : 0;
+#pragma unroll
+        for (int jj = 0; jj < 3; ++jj) {
+          const int j = 3 * h + jj;
+          if (nk && j < len) {
+            T G[9];
+#pragma unroll
+            for (int k = 0; k < 9; ++k) G[k] = Gs[(j * 9 + k) * kFanThreads + fl];
+            T u[4][DIM], fe[4][DIM];
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+              u[0][d] = uv[0][d];
+              u[1][d] = uv[1][d];
+              u[2][d] = uv[2 + jj][d];
+              u[3][d] = uv[3 + jj][d];
+            }
+            element_force<T, DIM>(u, G, P.lam, P.mu, P.cK, P.cM * P.mcoef[fe0 + j], fe);
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+              fv[0][d] += fe[0][d];
+              fv[1][d] += fe[1][d];
+              fv[2 + jj][d] += fe[2][d];
+              fv[3 + jj][d] += fe[3][d];
+            }
           }
         }
       }
-      if (MODE == MV_PCG) energy.add(e_fan);
+      if (MODE == MV_PCG) {  // p.Ap of this half-fan: sum over its node slots of u . f
+        T e_fan = 0;
+#pragma unroll
+        for (int k = 0; k < 6; ++k)
+#pragma unroll
+          for (int d = 0; d < DIM; ++d) e_fan += uv[k][d] * fv[k][d];
+        energy.add(e_fan);
+      }
     }
     __syncthreads();  // every thread has read its gradients: the G region becomes the force list
     T *fs = reinterpret_cast<T *>(B + L.g_off);

@@ -61,12 +61,12 @@ __global__ void __launch_bounds__(kHfanThreads) k_matvec_multi(MultiParams<float
   const FanBlockLayout &L = P.F.L;
   const int K = P.K;
   unsigned char *B = smem_raw;
-  T *fs = reinterpret_cast<T *>(smem_raw + L.bytes);                            // [R][kHalfSlots * kFanThreads][4]
+  // case-fastest layouts: the R cases of one node (or force slot) are adjacent
+  T *fs = reinterpret_cast<T *>(smem_raw + L.bytes);                            // [kHalfSlots * kFanThreads][R][4]
   constexpr int FS = kHalfSlots * kFanThreads * VW;
-  T *sp = fs + (size_t)R * FS;                                                  // [R][npn][4]
+  T *sp = fs + (size_t)R * FS;                                                  // [npn][R][4]
   uint64_t *bar = reinterpret_cast<uint64_t *>(sp + (size_t)R * L.npn * VW);
   double *s_en = reinterpret_cast<double *>(bar + 2);                           // [K] energies of this block
-  __shared__ int s_skip;
   if (MODE == MV_PCG && P.ctl->all_done) return;
   for (int c = threadIdx.x; c < K; c += blockDim.x) s_en[c] = 0;
   if (threadIdx.x == 0) {
@@ -100,13 +100,12 @@ __global__ void __launch_bounds__(kHfanThreads) k_matvec_multi(MultiParams<float
     const int nk = half_slot_count(h, len);
     for (int c0 = 0; c0 < K; c0 += R) {
       if (MODE == MV_PCG) {
-        if (threadIdx.x == 0) {
-          int all = 1;
-          for (int r = 0; r < R; ++r) all &= P.sc[c0 + r].done != 0;
-          s_skip = all;
-        }
-        __syncthreads();
-        if (s_skip) continue;  // uniform across the block
+        // every thread evaluates the pass's cases itself; the barrier's AND
+        // makes the decision uniform without a shared flag
+        int all = 1;
+#pragma unroll
+        for (int r = 0; r < R; ++r) all &= P.sc[c0 + r].done != 0;
+        if (__syncthreads_and(all)) continue;
       }
       // 1. stage: items (node i, case r), case fastest
       for (int q = threadIdx.x; q < nn * R; q += kHfanThreads) {
@@ -128,7 +127,7 @@ __global__ void __launch_bounds__(kHfanThreads) k_matvec_multi(MultiParams<float
         NodeV<T, VW> m;
 #pragma unroll
         for (int d = 0; d < VW; ++d) m.v[d] = (d < DIM && !(bb >> d & 1u)) ? v.v[d] : T(0);
-        stv<T, VW>(sp + (size_t)r * L.npn * VW, i, m);
+        stv<T, VW>(sp, (int64_t)i * R + r, m);
       }
       __syncthreads();
       // 2. half-fans, R cases per thread
@@ -144,7 +143,7 @@ __global__ void __launch_bounds__(kHfanThreads) k_matvec_multi(MultiParams<float
             NodeV<T, VW> s;
 #pragma unroll
             for (int d = 0; d < VW; ++d) s.v[d] = 0;
-            if (k < nk) s = ldv<T, VW>(sp + (size_t)r * L.npn * VW, li);
+            if (k < nk) s = ldv<T, VW>(sp, (int64_t)li * R + r);
 #pragma unroll
             for (int d = 0; d < DIM; ++d) {
               uv[r][k][d] = s.v[d];
@@ -193,7 +192,7 @@ __global__ void __launch_bounds__(kHfanThreads) k_matvec_multi(MultiParams<float
             NodeV<T, VW> o;
 #pragma unroll
             for (int d = 0; d < VW; ++d) o.v[d] = d < DIM ? fv[r][k][d] : T(0);
-            stv<T, VW>(fs + (size_t)r * FS, fpos[(h * 6 + k) * kFanThreads + fl], o);
+            stv<T, VW>(fs, (int64_t)fpos[(h * 6 + k) * kFanThreads + fl] * R + r, o);
           }
       __syncthreads();
       // 3. node sums: items (node i, case r)
@@ -202,11 +201,10 @@ __global__ void __launch_bounds__(kHfanThreads) k_matvec_multi(MultiParams<float
         const int i = q / R, r = q - i * R, c = c0 + r;
         const int g = nodes[i];
         const unsigned bb = bits[i];
-        const T *fr = fs + (size_t)r * FS;
         T acc[DIM] = {0, 0, 0};
         const int k1 = fstart[i + 1];
         for (int k = fstart[i]; k < k1; ++k) {
-          const NodeV<T, VW> fo = ldv<T, VW>(fr, k);
+          const NodeV<T, VW> fo = ldv<T, VW>(fs, (int64_t)k * R + r);
 #pragma unroll
           for (int d = 0; d < DIM; ++d) acc[d] += fo.v[d];
         }

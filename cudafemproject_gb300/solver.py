@@ -183,14 +183,15 @@ class FemContext:
         return out, self._info(inf)
 
     def pcg_multi(self, F, precision="fp64", tol=1e-8, stop_rule="reference", max_iter=1000000, outer_tol=1e-12,
-                  max_outer=50):
+                  max_outer=50, allow_not_converged=False):
+        """k load cases at once: F [k][n_dof] -> U [k][n_dof], per-case infos."""
         F = np.ascontiguousarray(F, dtype=np.float64)
         k = F.shape[0]
         U = np.zeros_like(F)
         prm = self._params(precision, tol, stop_rule, max_iter, outer_tol, max_outer)
         infos = (capi.SolveInfo * k)()
         st = capi.lib().cfem_pcg_multi(self._h, C.byref(prm), k, F.ctypes.data, U.ctypes.data, infos)
-        capi.check(st, "cfem_pcg_multi")
+        capi.check(st, "cfem_pcg_multi", (capi.OK, capi.ERR_NOT_CONVERGED) if allow_not_converged else (capi.OK,))
         return U, [self._info(i) for i in infos]
 
     def adjoint(self, u, dLdu, precision="fp64", tol=1e-12, stop_rule="residual", max_iter=1000000, outer_tol=1e-13,
