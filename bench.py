@@ -269,13 +269,12 @@ def main():
     achieved = byt.value / (msl.value * 1e-3) / 1e9
     msl64, byt64 = C.c_double(0), C.c_double(0)
     capi.check(L.cfem_profile_matvec(ctx._h, capi.FP64, 50, C.byref(msl64), C.byref(byt64)), "profile64")
-    traffic = None
-    tfile = os.path.join(REPO, "profiles", "matvec_fp32_traffic.json")
+    traffic = None  # DRAM bytes per launch of the same kernel on this workload, from a committed ncu summary
+    tfile = os.path.join(REPO, "profiles", "matvec_fp32_traffic.txt")
     if os.path.exists(tfile) and not args.small:
-        try:
-            traffic = json.load(open(tfile)).get("dram_bytes_per_launch")
-        except Exception:
-            traffic = None
+        for ln in open(tfile):
+            if ln.startswith("dram_bytes_per_launch"):
+                traffic = float(ln.split("=")[1])
     its = infos[-1]["iterations"]
     kernel_name = ("k_matvec_fan_tma<float,MV_PCG>" if ctx.counts()["matvec_form"] == capi.FORM_GRADIENT_FAN
                    else "k_matvec<float,3,MV_PCG>")
