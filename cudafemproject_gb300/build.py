@@ -29,7 +29,7 @@ NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xco
                   "-I", os.path.join(REPO, "include")]
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-ffp-contract=off", "-I", os.path.join(REPO, "include")]
 
-CU_SOURCES = ["context.cu", "context_dyn.cu", "context_multi.cu"]
+CU_SOURCES = ["context.cu", "context_dyn.cu", "context_multi.cu", "context_batch.cu"]
 CXX_SOURCES = ["prep.cpp", "femfunc.cpp"]
 
 

@@ -87,6 +87,9 @@ SIGNATURES = [
     ("cfem_static_solve", i32, [vp, C.POINTER(Wavelet), C.POINTER(SolveParams), vp, C.POINTER(SolveInfo)]),
     ("cfem_dyn", i32, [vp, C.POINTER(DynParams), C.POINTER(Wavelet), vp, C.POINTER(DynInfo)]),
     ("cfem_pcg_multi", i32, [vp, C.POINTER(SolveParams), i32, vp, vp, C.POINTER(SolveInfo)]),
+    ("cfem_create_batch", i32, [C.POINTER(vp), i32, C.POINTER(Mesh), C.POINTER(Material), C.POINTER(Options), vp]),
+    ("cfem_batch_info", i32, [vp, C.POINTER(i32), vp, vp]),
+    ("cfem_batch_static_solve", i32, [vp, C.POINTER(SolveParams), vp, C.POINTER(SolveInfo)]),
     ("cfem_adjoint", i32, [vp, C.POINTER(SolveParams), vp, vp, vp, vp, C.POINTER(SolveInfo)]),
     ("cfem_set_young", i32, [vp, vp]),
     ("cfem_dyn_adjoint", i32, [vp, C.POINTER(DynParams), C.POINTER(Wavelet), i32, vp, vp, C.POINTER(f64), vp,

@@ -41,6 +41,8 @@ MvParams<T> base_mv_t(cfem_ctx *c) {
 
 template <typename T>
 void launch_mv_t(cfem_ctx *c, int mode, const MvParams<T> &P) {
+  if (c->n_inst && !P.patch_inst)
+    throw Fail{CFEM_ERR_UNSUPPORTED, "a context of batched meshes supports cfem_batch_static_solve only"};
   // FP32: patch blocks streamed by bulk copies. FP64 keeps the plain fan
   // kernel below: it is bound by the FP64 pipe, and its twice-as-large blocks
   // would leave one CTA per SM.
@@ -405,7 +407,8 @@ void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, co
   int pe = opt && opt->patch_elems > 0 ? opt->patch_elems : (c->fans ? kFanMax * kFanThreads : 512);
   // the per-incidence force slots of a patch must fit in shared memory
   pe = std::min(std::max((pe + 31) / 32 * 32, 32), m->dim == 2 ? 2048 : 1024);
-  std::string err = build_prep(*m, pe, c->fans, c->prep);
+  if (c->n_inst && !c->fans) throw Fail{CFEM_ERR_UNSUPPORTED, "batched meshes need the 3D edge-fan form"};
+  std::string err = build_prep(*m, pe, c->fans, c->prep, c->elem_group.empty() ? nullptr : c->elem_group.data());
   if (!err.empty()) throw Fail{CFEM_ERR_MESH, err};
   err = build_rhs(*m, c->prep, c->semantics, c->rhs);
   if (!err.empty()) throw Fail{CFEM_ERR_MESH, err};
@@ -495,6 +498,42 @@ void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, co
     c->tma_err.alloc(1);
     c->tma_err.zero(s);
     CK(cudaMallocHost(&c->h_tma_err, sizeof(int)));
+  }
+  if (c->n_inst) {
+    // instance tables: patch -> instance, instance patch ranges, owned node ranges, materials
+    std::vector<int32_t> pinst(P.n_patches), ipo(c->n_inst + 1, 0), ofirst(P.n_patches + 1);
+    std::vector<float> pm32(2 * (size_t)P.n_patches);
+    std::vector<double> pm64(2 * (size_t)P.n_patches), le(c->ne), me(c->ne);
+    int64_t running = 0;
+    for (int p = 0; p < P.n_patches; ++p) {
+      pinst[p] = c->elem_group[P.elem_new2old[P.p_elem_off[p]]];
+      if (p && pinst[p] < pinst[p - 1]) throw Fail{CFEM_ERR_MESH, "internal error: batch patches out of order"};
+      ++ipo[pinst[p] + 1];
+      ofirst[p] = (int32_t)running;
+      const int nb = P.p_node_off[p], n = P.p_node_off[p + 1] - nb, own = P.p_own[p];
+      if (own < n && P.p_nodes[nb + own] != running) throw Fail{CFEM_ERR_MESH, "internal error: owned node ranges"};
+      running += n - own;
+      pm32[2 * p] = (float)c->inst_lam[pinst[p]];
+      pm32[2 * p + 1] = (float)c->inst_mu[pinst[p]];
+      pm64[2 * p] = c->inst_lam[pinst[p]];
+      pm64[2 * p + 1] = c->inst_mu[pinst[p]];
+    }
+    ofirst[P.n_patches] = (int32_t)running;
+    if (running != c->nn) throw Fail{CFEM_ERR_MESH, "internal error: owned node count"};
+    for (int i = 0; i < c->n_inst; ++i) ipo[i + 1] += ipo[i];
+    for (int64_t e = 0; e < c->ne; ++e) {
+      const int g = c->elem_group[P.elem_new2old[e]];
+      le[e] = c->inst_lam[g];
+      me[e] = c->inst_mu[g];
+    }
+    c->patch_inst.upload(pinst.data(), pinst.size(), s);
+    c->inst_patch_off.upload(ipo.data(), ipo.size(), s);
+    c->own_first.upload(ofirst.data(), ofirst.size(), s);
+    c->pmat32.upload(pm32.data(), pm32.size(), s);
+    c->pmat64.upload(pm64.data(), pm64.size(), s);
+    c->lam_e.upload(le.data(), le.size(), s);
+    c->mu_e.upload(me.data(), me.size(), s);
+    CK(cudaStreamSynchronize(s));
   }
   c->bits.upload(P.node_bits.data(), P.node_bits.size(), s);
   // coordinates and global connectivity in the new order (setup + checks)
@@ -662,6 +701,8 @@ void rebuild_operator(cfem_ctx *c) {
   gp.diag_local = nullptr;
   gp.elem_new2old = c->elem_new2old.p;
   gp.err = c->err.p;
+  gp.lam_e = c->lam_e.p;
+  gp.mu_e = c->mu_e.p;
   if (c->dim == 3) k_geometry<3><<<nblk(c->ne), kThreads, 0, s>>>(gp);
   else k_geometry<2><<<nblk(c->ne), kThreads, 0, s>>>(gp);
   CKL();
@@ -867,6 +908,7 @@ cfem_status cfem_renumbering(const cfem_ctx *ctx, int32_t *node_new2old, int32_t
 cfem_status cfem_element_matrices(cfem_ctx *ctx, int64_t first, int64_t count, double *ke) {
   return run_guarded([&]() -> cfem_status {
     check_ctx(ctx);
+    if (ctx->n_inst) throw Fail{CFEM_ERR_UNSUPPORTED, "not available for a context of batched meshes"};
     if (!ke || first < 0 || count < 0 || first + count > ctx->ne) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "bad element range"};
     if (count == 0) return CFEM_OK;
     DBuf<double> out;
@@ -1159,6 +1201,10 @@ extern "C" cfem_status cfem_matvec_energy_noalloc(cfem_ctx *ctx, const double *x
   if (cudaGetDevice(&dev) != cudaSuccess || dev != ctx->device) {
     g_last_error = "cfem_matvec_energy_noalloc: the context's device must be current";
     return CFEM_ERR_INVALID_ARGUMENT;
+  }
+  if (ctx->n_inst) {
+    g_last_error = "cfem_matvec_energy_noalloc: not available for a context of batched meshes";
+    return CFEM_ERR_UNSUPPORTED;
   }
   if (ctx->grid_mv > kNoAllocMaxBlocks) {
     g_last_error = "cfem_matvec_energy_noalloc: the context needs " + std::to_string(ctx->grid_mv) +

@@ -541,6 +541,7 @@ cfem_status cfem_adjoint(cfem_ctx *ctx, const cfem_solve_params *prm, const doub
 cfem_status cfem_element_stress(cfem_ctx *ctx, const double *u, double *strain, double *stress, double *mises) {
   return run_guarded([&]() -> cfem_status {
     check_ctx(ctx);
+    if (ctx->n_inst) throw Fail{CFEM_ERR_UNSUPPORTED, "not available for a context of batched meshes"};
     if (!u) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "null displacement"};
     enter(ctx);
     const int S = 3 * (ctx->dim - 1);
@@ -571,6 +572,7 @@ cfem_status cfem_element_stress(cfem_ctx *ctx, const double *u, double *strain, 
 cfem_status cfem_set_young(cfem_ctx *ctx, const double *elem_young) {
   return run_guarded([&]() -> cfem_status {
     check_ctx(ctx);
+    if (ctx->n_inst) throw Fail{CFEM_ERR_UNSUPPORTED, "not available for a context of batched meshes"};
     enter(ctx);
     if (!elem_young) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "null array"};
     std::vector<double> yv(ctx->ne);

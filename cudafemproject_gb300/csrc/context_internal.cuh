@@ -17,6 +17,7 @@
 #include "kernels_fan.cuh"
 #include "kernels_fan_tma.cuh"
 #include "kernels_multi.cuh"
+#include "kernels_batch.cuh"
 #include "prep.hpp"
 
 namespace cfem {
@@ -155,6 +156,14 @@ struct cfem_ctx {
   size_t smem64 = 0, smem32 = 0;
   int chunk = 16;
   MultiState *multi = nullptr;
+  // batch of independent meshes (cfem_create_batch); n_inst == 0 for one mesh
+  int n_inst = 0;
+  std::vector<int32_t> elem_group;               // caller element -> instance
+  std::vector<double> inst_lam, inst_mu;
+  std::vector<int64_t> inst_node_off, inst_elem_off;  // caller order
+  DBuf<int32_t> patch_inst, inst_patch_off, own_first;
+  DBuf<float> pmat32;
+  DBuf<double> pmat64, lam_e, mu_e;
   int64_t launches = 0;  // kernels issued since the counter was last reset
   GraphCache graph64, graph32;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -211,6 +220,8 @@ void enter(cfem_ctx *c);
 cfem_solve_params default_params();
 cfem_status solve_internal(cfem_ctx *c, const cfem_solve_params *prm, cfem_solve_info *info);
 void rebuild_operator(cfem_ctx *c);
+void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, const cfem_options *opt);
+void attach_stream(cfem_ctx *c, cudaStream_t s);
 
 template <typename T>
 inline MvParams<T> base_mv(cfem_ctx *c) {

@@ -208,6 +208,32 @@ struct DotAcc<float> {
   __device__ __forceinline__ void add(float v) { c.add(v); }
 };
 
+// Block total of one accumulator per thread (all threads call; valid in thread 0).
+template <typename T>
+__device__ __forceinline__ double block_total(const DotAcc<T> &a) {
+  __shared__ double red_bt[kThreads / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  double w;
+  if constexpr (sizeof(T) == 8) {
+    w = a.s;
+    for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(0xffffffffu, w, o);
+  } else {
+    Comp32 c = a.c;
+    for (int o = 16; o > 0; o >>= 1) {
+      const float h2 = __shfl_down_sync(0xffffffffu, c.hi, o), l2 = __shfl_down_sync(0xffffffffu, c.lo, o);
+      c.merge(h2, l2);
+    }
+    w = (double)c.hi + (double)c.lo;
+  }
+  if (lane == 0) red_bt[wid] = w;
+  __syncthreads();
+  double t = 0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += red_bt[i];
+  __syncthreads();
+  return t;
+}
+
 // Grid sum of N accumulators per thread; true in thread 0 of the last block,
 // whose v then holds the totals.
 template <int N, typename T>
@@ -321,6 +347,12 @@ __device__ __forceinline__ void tet_forces_rel(const T (&d1)[3], const T (&d2)[3
 // ------------------------------------------------------------------ matvec
 enum MvMode { MV_PLAIN = 0, MV_PCG = 1, MV_DYN = 2 };
 
+// Control block of a batched solve (independent meshes).
+struct BatchCtl {
+  int iter, all_done;
+  unsigned int count_mv, count_up;
+};
+
 template <typename T>
 struct MvParams {
   int n_patches;
@@ -342,7 +374,35 @@ struct MvParams {
   T c1, c2;          // DYN: d_new = d + c1 v + c2 a
   const uint16_t *inc, *inc_start;  // per-patch incidence lists (prep.hpp)
   int pe, np_max;    // element slots per patch, node slots per patch (multiple of 4)
+  // batch of independent meshes (all nullptr for a single mesh): every patch
+  // belongs to one instance with its own material and PCG scalars
+  const int32_t *patch_inst;      // [n_patches]
+  const T *pmat;                  // [n_patches][2]: lambda, mu
+  Scalars *isc;                   // [n_inst] per-instance PCG scalars
+  BatchCtl *bctl;
+  double *patch_energy;           // [n_patches] per-patch p.Ap
+  const int32_t *inst_patch_off;  // [n_inst + 1]
+  int n_inst;
 };
+
+// Last-block helper for batches: per instance i, the sum of vals[p*stride + k]
+// over its contiguous patch range, one warp per instance (strided lane sums
+// and a shuffle tree: a fixed order). Called by all threads of one block.
+template <int N>
+__device__ __forceinline__ void instance_sums(const double *vals, int stride, const int32_t *inst_patch_off, int n_inst,
+                                              double *out /* [n_inst][N] */) {
+  const int lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
+  for (int i = threadIdx.x >> 5; i < n_inst; i += nwarp) {
+    const int p0 = inst_patch_off[i], p1 = inst_patch_off[i + 1];
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      double s = 0;
+      for (int p = p0 + lane; p < p1; p += 32) s += __ldcg(vals + (size_t)p * stride + k);
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+      if (lane == 0) out[(size_t)i * N + k] = s;
+    }
+  }
+}
 
 // One CTA per patch (grid-stride over patches). Three phases per patch:
 //  1. stage: the patch's node values (PCG: p = z + beta p_old, written back for

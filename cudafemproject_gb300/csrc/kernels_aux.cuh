@@ -26,6 +26,7 @@ struct GeomParams {
   double *diag_local;     // [ne][w] element diagonal of K in original element/slot order (or nullptr)
   const int32_t *elem_new2old;
   int *err;
+  const double *lam_e, *mu_e;  // per-element material (new order) or nullptr
 };
 
 template <int DIM>
@@ -107,7 +108,8 @@ __global__ void k_geometry(GeomParams P) {
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
       // D = lam 1(x)1 + 2 mu I (Voigt, engineering shear): diag of B^T D B
-      double kd = (P.lam + 2 * P.mu) * sq[d] + P.mu * (tot - sq[d]);
+      const double lam = P.lam_e ? P.lam_e[e] : P.lam, mu = P.mu_e ? P.mu_e[e] : P.mu;
+      double kd = (lam + 2 * mu) * sq[d] + mu * (tot - sq[d]);
       atomicAdd(P.diagK + (int64_t)v[a] * VW + d, kd);
       if (P.mlump) atomicAdd(P.mlump + (int64_t)v[a] * VW + d, P.lump_c * mass);
       if (P.diag_local) P.diag_local[eo * W + DIM * a + d] = kd;

@@ -47,6 +47,7 @@ __global__ void __launch_bounds__(kFanThreads) k_matvec_fan(MvParams<T> P, FanPa
   for (int patch = blockIdx.x; patch < P.n_patches; patch += gridDim.x) {
     const int nb = P.node_off[patch], nn = P.node_off[patch + 1] - nb, own = P.own[patch];
     const int f0 = F.fan_off[patch], nf = F.fan_off[patch + 1] - f0;
+    const T lam = P.patch_inst ? P.pmat[2 * patch] : P.lam, mu = P.patch_inst ? P.pmat[2 * patch + 1] : P.mu;
     // 1. stage: incidence codes (kFanSlots per fan, 4-byte aligned), offsets, node values
     {
       const uint32_t *src = reinterpret_cast<const uint32_t *>(F.finc + (size_t)kFanSlots * f0);
@@ -112,7 +113,7 @@ __global__ void __launch_bounds__(kFanThreads) k_matvec_fan(MvParams<T> P, FanPa
             u[3][d] = uv[3 + j][d];
           }
           const T mc = P.mcoef ? P.cM * P.mcoef[fe0 + j] : T(0);
-          element_force<T, DIM>(u, G, P.lam, P.mu, P.cK, mc, fe);
+          element_force<T, DIM>(u, G, lam, mu, P.cK, mc, fe);
 #pragma unroll
           for (int d = 0; d < DIM; ++d) {
             if (MODE == MV_PCG) e_fan += u[0][d] * fe[0][d] + u[1][d] * fe[1][d] + u[2][d] * fe[2][d] + u[3][d] * fe[3][d];

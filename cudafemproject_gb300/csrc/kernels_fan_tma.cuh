@@ -74,9 +74,11 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
   unsigned char *buf0 = smem_raw, *buf1 = smem_raw + L.bytes;
   T *sp = reinterpret_cast<T *>(smem_raw + 2 * (size_t)L.bytes);  // [npn][4] staged node values
   uint64_t *bar = reinterpret_cast<uint64_t *>(sp + (size_t)L.npn * VW);
-  if (MODE == MV_PCG && P.sc->done) return;
+  const bool batch = P.patch_inst != nullptr;
+  if (MODE == MV_PCG && (batch ? P.bctl->all_done : P.sc->done)) return;
   T beta = 0;
-  if (MODE == MV_PCG) beta = T(P.sc->beta);
+  if (MODE == MV_PCG && !batch) beta = T(P.sc->beta);
+  T lam = P.lam, mu = P.mu;
   if (threadIdx.x == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
@@ -114,6 +116,17 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
     const T *Gs = reinterpret_cast<const T *>(B + L.g_off);
     const int nn = P.node_off[patch + 1] - P.node_off[patch], own = P.own[patch];
     const int nf = F.fan_off[patch + 1] - F.fan_off[patch];
+    bool skip = false;
+    if (batch) {  // the patch's instance: material, direction update, convergence mask
+      lam = P.pmat[2 * patch];
+      mu = P.pmat[2 * patch + 1];
+      if (MODE == MV_PCG) {
+        const Scalars &si = P.isc[P.patch_inst[patch]];
+        skip = si.done != 0;
+        beta = T(si.beta);
+      }
+    }
+    if (!skip) {
     // 1. stage node values: each thread issues the gathers of all its nodes
     //    (up to kStageUnroll) before using any of them
     constexpr int SU = kStageUnroll;
@@ -175,7 +188,7 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
         }
       }
       if (P.mcoef == nullptr) {
-        const T lamk = P.lam * P.cK, muk = P.mu * P.cK;
+        const T lamk = lam * P.cK, muk = mu * P.cK;
         T du[6][DIM];
 #pragma unroll
         for (int k = 1; k < 6; ++k)
@@ -289,6 +302,12 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
       }
       if (any) atomic_addv<T, VW>(P.y, g, r, DIM);
     }
+    }  // !skip
+    if (MODE == MV_PCG && batch) {  // p.Ap per patch; summed per instance at the end
+      const double t = block_total<T>(energy);
+      if (threadIdx.x == 0) P.patch_energy[patch] = t;
+      energy = DotAcc<T>();
+    }
     // Buffer b is free again. Every thread orders its own generic-proxy
     // accesses of it (the force stores and reads) before the bulk copy that
     // refills it, then the barrier makes that true for all of them.
@@ -299,13 +318,31 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
       bulk_load(B, F.blocks + (size_t)(patch + 2 * step) * L.bytes, (unsigned)L.bytes, &bar[b]);
     }
   }
-  if (MODE == MV_PCG) {
+  if (MODE == MV_PCG && !batch) {
     DotAcc<T> ea[1] = {energy};
     double v[1];
     if (grid_sum_acc<1, T>(ea, v, P.partials, &P.sc->count_mv)) {
       P.sc->sigma = v[0];
       P.sc->alpha = P.sc->gamma / v[0];
     }
+  } else if (MODE == MV_PCG) {  // per-instance sigma and alpha from the per-patch sums
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(&P.bctl->count_mv, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    instance_sums<1>(P.patch_energy, 1, P.inst_patch_off, P.n_inst, P.partials);
+    __syncthreads();
+    for (int i = threadIdx.x; i < P.n_inst; i += blockDim.x) {
+      Scalars &si = P.isc[i];
+      if (!si.done) {
+        si.sigma = P.partials[i];
+        si.alpha = si.gamma / si.sigma;
+      }
+    }
+    if (threadIdx.x == 0) P.bctl->count_mv = 0;
   }
 }
 

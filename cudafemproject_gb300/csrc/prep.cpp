@@ -34,7 +34,7 @@ inline uint64_t spread2(uint64_t v) {  // 32 bits -> every second bit
 
 }  // namespace
 
-std::string build_prep(const cfem_mesh &m, int patch_elems, bool use_fans, Prep &P) {
+std::string build_prep(const cfem_mesh &m, int patch_elems, bool use_fans, Prep &P, const int32_t *elem_group) {
   const int dim = m.dim;
   if (dim != 2 && dim != 3) return "dim must be 2 or 3";
   if (m.n_nodes <= 0 || m.n_elems <= 0) return "mesh has no nodes or no elements";
@@ -85,6 +85,12 @@ std::string build_prep(const cfem_mesh &m, int patch_elems, bool use_fans, Prep 
     key[e] = {k, (int32_t)e};
   }
   std::sort(key.begin(), key.end());
+  // independent meshes of a batch stay apart: group first, locality order inside a group
+  if (elem_group)
+    std::stable_sort(key.begin(), key.end(), [&](const std::pair<uint64_t, int32_t> &a,
+                                                 const std::pair<uint64_t, int32_t> &b) {
+      return elem_group[a.second] < elem_group[b.second];
+    });
   P.elem_new2old.resize(ne);
   P.elem_old2new.resize(ne);
   for (int64_t i = 0; i < ne; ++i) {
@@ -230,8 +236,9 @@ std::string build_prep(const cfem_mesh &m, int patch_elems, bool use_fans, Prep 
       P.p_fan_off.push_back((int32_t)f);
       P.p_elem_off.push_back(P.fan_elem_off[f]);
       int64_t f1 = f;
+      auto group_of = [&](int64_t fan) { return elem_group ? elem_group[P.elem_new2old[P.fan_elem_off[fan]]] : 0; };
       while (f1 < P.n_fans && (f1 - f) < (P.fans ? kFanThreads : pe) &&
-             P.fan_elem_off[f1 + 1] - P.fan_elem_off[f] <= pe)
+             P.fan_elem_off[f1 + 1] - P.fan_elem_off[f] <= pe && group_of(f1) == group_of(f))
         ++f1;
       f = f1;
     }

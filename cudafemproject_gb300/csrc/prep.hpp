@@ -61,7 +61,10 @@ struct Prep {
 };
 
 // Returns an empty string on success, else the error message.
-std::string build_prep(const cfem_mesh &m, int patch_elems, bool use_fans, Prep &out);
+// elem_group (optional, per element): elements of different groups never share
+// a patch and are ordered group by group (independent meshes of a batch).
+std::string build_prep(const cfem_mesh &m, int patch_elems, bool use_fans, Prep &out,
+                       const int32_t *elem_group = nullptr);
 
 // Wavelet value in the reference's float arithmetic (fem_utils.cpp:53-82).
 float wavelet_value(const cfem_wavelet *w, float t);

@@ -148,6 +148,20 @@ def random_tets(n_points: int = 800, seed: int = 7, E: float = 2e7, nu: float = 
                    face_normal=np.zeros((0, 3)), face_pressure=np.zeros(0), E=E, nu=nu, rho=rho)
 
 
+def batch_boxes(n_boxes: int = 64, seed: int = 2, n_min: int = 8, n_max: int = 40, jitter: float = 0.2):
+    """Independent tet boxes n x n x 4n (aspect 1:1:4, side counts uniform in
+    [n_min, n_max]), each with E log-uniform in [1e6, 1e8] and nu uniform in
+    [0.2, 0.4]; face z=0 clamped, traction 1e3 in -y on the top face; interior
+    nodes jittered by +-jitter h (box i uses seed + 1 + i). Draw order: all
+    side counts, then all E, then all nu."""
+    rng = np.random.default_rng(seed)
+    ns = rng.integers(n_min, n_max + 1, size=n_boxes)
+    Es = 10.0 ** rng.uniform(6, 8, size=n_boxes)
+    nus = rng.uniform(0.2, 0.4, size=n_boxes)
+    return [box_3d(int(n), int(n), 4 * int(n), jitter=jitter, seed=seed + 1 + i, E=float(E), nu=float(nu),
+                   traction=(0.0, -1e3, 0.0)) for i, (n, E, nu) in enumerate(zip(ns, Es, nus))]
+
+
 def cantilever_1p39m(seed: int = 0) -> Problem:
     """1x1x4 box, 48x48x192 hexes x 6 tets (2,654,208 tets, 1,390,179 DOF), jitter 0.2h."""
     return box_3d(48, 48, 192, jitter=0.2, seed=seed, traction=(0.0, -1e3, 0.0))

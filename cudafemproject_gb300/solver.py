@@ -40,6 +40,23 @@ def _wavelet(w: Optional[WaveletParams]):
     return capi.Wavelet(int(w.code), float(w.freq), float(w.timeshift), float(w.ampl))
 
 
+def _mesh_struct(p: Problem):
+    """cfem_mesh view of a Problem; the returned dict keeps its arrays alive."""
+    c = lambda a, dt: np.ascontiguousarray(a, dtype=dt)
+    k = dict(
+        nodes=c(p.nodes, np.float64), elems=c(p.elems, np.int32), cons=c(p.cons.reshape(-1, 2), np.int32),
+        lnode=c(p.load_node, np.int32), lvec=c(p.load_vec.reshape(-1, p.dim) if len(p.load_node) else np.zeros((0, p.dim)), np.float64),
+        fnodes=c(p.face_nodes.reshape(-1, p.dim + 1), np.int32), felem=c(p.face_elem, np.int32),
+        fnorm=c(p.face_normal.reshape(-1, p.dim) if len(p.face_elem) else np.zeros((0, p.dim)), np.float64),
+        fpress=c(p.face_pressure, np.float64),
+        young=None if p.elem_E is None else c(p.elem_E, np.float64))
+    pz = lambda a: a.ctypes.data if a is not None and a.size else None
+    mesh = capi.Mesh(p.dim, p.n_nodes, pz(k["nodes"]), p.n_elems, pz(k["elems"]), len(k["cons"]), pz(k["cons"]),
+                     len(k["lnode"]), pz(k["lnode"]), pz(k["lvec"]), len(k["felem"]), pz(k["fnodes"]),
+                     pz(k["felem"]), pz(k["fnorm"]), pz(k["fpress"]), pz(k["young"]))
+    return mesh, k
+
+
 class FemContext:
     """One mesh on the current GPU. ``semantics`` is "compat" (reproduce the
     reference, quirks included) or "consistent" (textbook operators/loads)."""
@@ -53,19 +70,7 @@ class FemContext:
         self.ndof = p.n_dof
         self.w = 6 * (p.dim - 1)
         L = capi.lib()
-        c = lambda a, dt: np.ascontiguousarray(a, dtype=dt)
-        self._keep = dict(
-            nodes=c(p.nodes, np.float64), elems=c(p.elems, np.int32), cons=c(p.cons.reshape(-1, 2), np.int32),
-            lnode=c(p.load_node, np.int32), lvec=c(p.load_vec.reshape(-1, p.dim) if len(p.load_node) else np.zeros((0, p.dim)), np.float64),
-            fnodes=c(p.face_nodes.reshape(-1, p.dim + 1), np.int32), felem=c(p.face_elem, np.int32),
-            fnorm=c(p.face_normal.reshape(-1, p.dim) if len(p.face_elem) else np.zeros((0, p.dim)), np.float64),
-            fpress=c(p.face_pressure, np.float64),
-            young=None if p.elem_E is None else c(p.elem_E, np.float64))
-        k = self._keep
-        pz = lambda a: a.ctypes.data if a is not None and a.size else None
-        mesh = capi.Mesh(p.dim, p.n_nodes, pz(k["nodes"]), p.n_elems, pz(k["elems"]), len(k["cons"]), pz(k["cons"]),
-                         len(k["lnode"]), pz(k["lnode"]), pz(k["lvec"]), len(k["felem"]), pz(k["fnodes"]),
-                         pz(k["felem"]), pz(k["fnorm"]), pz(k["fpress"]), pz(k["young"]))
+        mesh, self._keep = _mesh_struct(p)
         mat = capi.Material(float(p.E), float(p.nu), float(p.rho))
         form = {"gradient": capi.FORM_GRADIENT, "stored_ke": capi.FORM_STORED_KE, "auto": capi.FORM_AUTO,
                 "fan": capi.FORM_GRADIENT_FAN}[matvec_form]
@@ -255,3 +260,60 @@ class FemContext:
         if trace is not None:
             return u.reshape(-1, self.dim), info, trace
         return u.reshape(-1, self.dim), info
+
+
+class BatchContext:
+    """Independent 3D meshes, each with its own material, solved together
+    (cfem_create_batch): one set of kernel launches for all instances, with a
+    per-instance stopping test. ``problems`` is a list of Problem."""
+
+    def __init__(self, problems, semantics: str = "consistent", stream=None, patch_elems: int = 0,
+                 verbose: bool = False):
+        self.problems = list(problems)
+        n = len(self.problems)
+        meshes = (capi.Mesh * n)()
+        mats = (capi.Material * n)()
+        self._keep = []
+        for i, p in enumerate(self.problems):
+            if p.dim != 3:
+                raise ValueError("batched meshes must be 3D")
+            m, k = _mesh_struct(p)
+            meshes[i] = m
+            mats[i] = capi.Material(float(p.E), float(p.nu), float(p.rho))
+            self._keep.append(k)
+        opt = capi.Options({"compat": capi.COMPAT, "consistent": capi.CONSISTENT}[semantics], capi.FORM_AUTO,
+                           int(patch_elems), int(verbose))
+        h = C.c_void_p()
+        st = capi.lib().cfem_create_batch(C.byref(h), n, meshes, mats, C.byref(opt), stream)
+        capi.check(st, "cfem_create_batch")
+        self._h = h
+        self.n = n
+        self.node_off = np.zeros(n + 1, np.int64)
+        self.elem_off = np.zeros(n + 1, np.int64)
+        cnt = C.c_int32(0)
+        capi.check(capi.lib().cfem_batch_info(self._h, C.byref(cnt), self.node_off.ctypes.data,
+                                              self.elem_off.ctypes.data), "cfem_batch_info")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            capi.lib().cfem_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def static_solve(self, precision="fp32_refine", tol=1e-4, stop_rule="residual", max_iter=1000000,
+                     outer_tol=1e-10, max_outer=50, allow_not_converged=False):
+        """Every instance under its own loads; returns ([u_i [n_nodes_i, 3]], [info_i])."""
+        u = np.zeros(int(self.node_off[-1]) * 3, np.float64)
+        prm = FemContext._params(precision, tol, stop_rule, max_iter, outer_tol, max_outer)
+        infos = (capi.SolveInfo * self.n)()
+        st = capi.lib().cfem_batch_static_solve(self._h, C.byref(prm), u.ctypes.data, infos)
+        capi.check(st, "cfem_batch_static_solve",
+                   (capi.OK, capi.ERR_NOT_CONVERGED) if allow_not_converged else (capi.OK,))
+        us = [u[3 * self.node_off[i]:3 * self.node_off[i + 1]].reshape(-1, 3) for i in range(self.n)]
+        return us, [FemContext._info(i) for i in infos]
+

@@ -220,6 +220,24 @@ CFEM_API cfem_status cfem_adjoint(cfem_ctx *ctx, const cfem_solve_params *prm, c
  * receives the displacements. Keys under "gb300" select precision/semantics. */
 CFEM_API cfem_status cfem_run_task(const char *config_path, const char *task, int32_t write_vtk, double *u_out,
                                    int64_t n_out, cfem_solve_info *static_info, cfem_dyn_info *dyn_info);
+/* Batched independent meshes (no counterpart in the reference, which solves
+ * one mesh per process): n 3D meshes, each with its own material, in one
+ * context. Node, element, constraint, load and face arrays are each mesh's
+ * own (0-based per mesh); the batch concatenates them instance after instance
+ * (cfem_batch_info gives the offsets). Only cfem_batch_static_solve and the
+ * structural queries accept such a context; CFEM_ERR_UNSUPPORTED otherwise. */
+CFEM_API cfem_status cfem_create_batch(cfem_ctx **out, int32_t n, const cfem_mesh *meshes, const cfem_material *mats,
+                                       const cfem_options *opt, void *stream);
+/* n instances; node_off / elem_off (may be NULL) receive n + 1 offsets into
+ * the concatenated caller order. */
+CFEM_API cfem_status cfem_batch_info(const cfem_ctx *ctx, int32_t *n, int64_t *node_off, int64_t *elem_off);
+/* Static solve of every instance under its own loads, all instances in the
+ * same kernel launches with per-instance PCG scalars and stopping tests (a
+ * converged instance is skipped). prm->precision CFEM_FP32 or CFEM_FP32_REFINE
+ * (per-instance FP64 refinement). u: concatenated displacements (n_dof of all
+ * instances); info: NULL or [n]. */
+CFEM_API cfem_status cfem_batch_static_solve(cfem_ctx *ctx, const cfem_solve_params *prm, double *u,
+                                             cfem_solve_info *info);
 /* Measurement: n back-to-back launches of the PCG-form matvec kernel (direction
  * update + element operator + scatter + p.Ap reduction) on the context's stream,
  * timed with CUDA events. Returns the mean device time per launch and the
