@@ -141,6 +141,183 @@ def run_reference(args):
     return 0
 
 
+def _line(metric, value, unit, higher, config, extra):
+    line = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "higher_is_better": higher,
+            "data": "synthetic (seeded mesh generator, see config)", "config": config}
+    line.update(extra)
+    print(json.dumps(line), flush=True)
+
+
+def run_other_workload(args):
+    """Measurements of the other configurations (not the driver's headline)."""
+    import torch
+    torch.cuda.set_device(0)
+    from cudafemproject_gb300 import meshgen
+    from cudafemproject_gb300.solver import BatchContext, FemContext
+    if args.workload == "multi_rhs":
+        # 24x24x96 tet box; each case a traction on z = max, direction uniform on the
+        # sphere, magnitude log-uniform in [1e2, 1e4] (seed 1: k directions, then k magnitudes)
+        nx, ny, nz = 24, 24, 96
+        E3 = np.stack([FemContext(meshgen.box_3d(nx, ny, nz, traction=t), semantics="consistent").rhs()
+                       for t in ((1.0, 0, 0), (0, 1.0, 0), (0, 0, 1.0))])
+        ctx = FemContext(meshgen.box_3d(nx, ny, nz), semantics="consistent")
+        kw = dict(precision="fp32_refine", tol=1e-4, stop_rule="residual", outer_tol=1e-8, max_iter=20000)
+        rng = np.random.default_rng(1)
+        for k in (64, 256):
+            d = rng.standard_normal((k, 3))
+            d /= np.linalg.norm(d, axis=1, keepdims=True)
+            F = (d * (10.0 ** rng.uniform(2, 4, size=k))[:, None]) @ E3
+            ctx.pcg_multi(F, **kw)
+            U, infos = ctx.pcg_multi(F, **kw)
+            ms_multi = infos[0]["solve_ms"]
+            single = [ctx.pcg(F[i], **kw)[1]["solve_ms"] for i in range(4)]
+            ms_single = float(np.mean(single[1:]))
+            err = max(float(np.linalg.norm(U[i] - ctx.pcg(F[i], "fp64", tol=1e-12, stop_rule="residual")[0].ravel())
+                            / np.linalg.norm(U[i])) for i in range(2))
+            _line("multi-RHS solve time per load case to 1e-8 rel err", round(ms_multi / k, 3), "ms", False,
+                  {"workload": f"24x24x96 tet box (331,776 tets, 181,875 DOF), {k} traction load cases",
+                   "precision": "FP32 inner PCG + FP64 refinement"},
+                  {"batched_ms_total": round(ms_multi, 1), "single_rhs_ms": round(ms_single, 3),
+                   "per_rhs_speedup": round(ms_single / (ms_multi / k), 2), "rel_err_vs_fp64": err})
+    elif args.workload == "batch":
+        probs = meshgen.batch_boxes(64, seed=2)
+        kw = dict(precision="fp32_refine", tol=1e-4, outer_tol=1e-8, max_iter=20000)
+        b = BatchContext(probs)
+        b.static_solve(**kw)
+        us, infos = b.static_solve(**kw)
+        ms_b = infos[0]["solve_ms"]
+        b.close()
+        seq, errs = 0.0, []
+        for i, p in enumerate(probs):
+            ctx = FemContext(p, semantics="consistent")
+            ctx.static_solve(stop_rule="residual", **kw)
+            u1, inf = ctx.static_solve(stop_rule="residual", **kw)
+            seq += inf["solve_ms"]
+            if i < 4:
+                ref, _ = ctx.static_solve("fp64", tol=1e-13, stop_rule="residual", max_iter=40000,
+                                          allow_not_converged=True)
+                errs.append(float(np.linalg.norm(us[i] - ref) / np.linalg.norm(ref)))
+            ctx.close()
+        _line("batched independent meshes: solve time of all instances to 1e-8 rel err", round(ms_b, 1), "ms", False,
+              {"workload": f"64 tet boxes n x n x 4n, n uniform in 8..40 (seed 2), E log-uniform [1e6, 1e8], "
+                           f"nu uniform [0.2, 0.4]: {sum(p.n_elems for p in probs)} tets, "
+                           f"{sum(p.n_dof for p in probs)} DOF", "precision": "FP32 inner PCG + FP64 refinement"},
+              {"sequential_single_mesh_ms": round(seq, 1), "speedup_vs_sequential": round(seq / ms_b, 3),
+               "max_iterations": max(i["iterations"] for i in infos), "rel_err_vs_fp64_first4": max(errs)})
+    elif args.workload == "adjoint":
+        run_adjoint_workload()
+    elif args.workload == "dynamics":
+        run_dynamics_workload()
+    return 0
+
+
+def run_adjoint_workload():
+    """Tet cantilever 32x32x128 x 6 (786,432 tets), E_e = 2e7 exp(0.5 z_e) (seed 3),
+    loss = f.u + 1/2 sum over 500 surface sensors |u_s - u_obs|^2, u_obs from a
+    second field (seed 4). Gradient by the adjoint; checked by central finite
+    differences along a random direction and on the 20 elements of largest
+    sensitivity (relative step 1e-4)."""
+    from cudafemproject_gb300 import meshgen
+    from cudafemproject_gb300.solver import FemContext
+    p = meshgen.box_3d(32, 32, 128, traction=(0.0, -1e3, 0.0))
+    rng = np.random.default_rng(3)
+    young = 2e7 * np.exp(0.5 * rng.standard_normal(p.n_elems))
+    surf = np.nonzero((p.nodes[:, 0] <= 1e-9) | (p.nodes[:, 0] >= 1 - 1e-9) | (p.nodes[:, 1] <= 1e-9) |
+                      (p.nodes[:, 1] >= 1 - 1e-9) | (p.nodes[:, 2] >= 4 - 1e-9))[0]
+    sensors = rng.choice(surf, size=500, replace=False)
+    young_obs = 2e7 * np.exp(0.5 * np.random.default_rng(4).standard_normal(p.n_elems))
+    kw = dict(precision="fp32_refine", tol=1e-4, stop_rule="residual", outer_tol=1e-13, max_iter=40000)
+    p.elem_E = young_obs
+    ctx = FemContext(p, semantics="consistent")
+    f = ctx.rhs()
+    u_obs = ctx.pcg(f, **kw)[0].reshape(-1, 3)[sensors]
+    ctx.set_young(young)
+
+    def loss(u):
+        u = u.reshape(-1, 3)
+        return float(f @ u.ravel() + 0.5 * np.sum((u[sensors] - u_obs) ** 2))
+
+    u, inf_f = ctx.pcg(f, **kw)
+    g = f.copy().reshape(-1, 3)
+    g[sensors] += u.reshape(-1, 3)[sensors] - u_obs
+    dE, _, inf_a = ctx.adjoint(u, g.ravel(), **kw)
+    t_total = inf_f["solve_ms"] + inf_a["solve_ms"]
+    # central differences
+    rng2 = np.random.default_rng(7)
+    v = rng2.standard_normal(p.n_elems) * young
+    h = 1e-4
+    ctx.set_young(young + h * v)
+    lp = loss(ctx.pcg(f, **kw)[0])
+    ctx.set_young(young - h * v)
+    lm = loss(ctx.pcg(f, **kw)[0])
+    fd_dir = (lp - lm) / (2 * h)
+    ad_dir = float(dE @ v)
+    errs = []
+    for e in np.argsort(-np.abs(dE * young))[:20]:
+        y = young.copy()
+        y[e] *= 1 + h
+        ctx.set_young(y)
+        lp = loss(ctx.pcg(f, **kw)[0])
+        y[e] = young[e] * (1 - h)
+        ctx.set_young(y)
+        lm = loss(ctx.pcg(f, **kw)[0])
+        fd = (lp - lm) / (2 * h * young[e])
+        errs.append(abs(fd - dE[e]) / abs(dE[e]))
+    ctx.set_young(young)
+    _line("adjoint gradient: forward + adjoint solve time", round(t_total, 2), "ms", False,
+          {"workload": "tet cantilever 32x32x128 x 6 (786,432 tets, 421,443 DOF), E_e = 2e7 exp(0.5 z_e) seed 3, "
+                       "loss f.u + 1/2 |u_s - u_obs|^2 at 500 surface sensors, u_obs from field seed 4",
+           "precision": "FP32 inner PCG + FP64 refinement to true rel. residual 1e-13"},
+          {"forward_ms": round(inf_f["solve_ms"], 2), "adjoint_ms": round(inf_a["solve_ms"], 2),
+           "fd_directional_rel_err": abs(fd_dir - ad_dir) / abs(ad_dir),
+           "fd_20_elements_max_rel_err": max(errs), "fd_20_elements_median_rel_err": float(np.median(errs))})
+
+
+def run_dynamics_workload():
+    """Tet column 1x1x8, 32x32x256 x 6 (1,572,864 tets), rho 2000, E 2e7, nu 0.25,
+    base clamped, Ricker point force (25 Hz, -z) at the top centre. Explicit
+    central difference (lumped mass) at 0.5 x the stability limit from 100
+    power iterations on M_L^-1 K (seed 5), 5000 steps; implicit Newmark
+    beta 0.25 gamma 0.5 (GN22 beta1 = beta2 = 0.5), dt 1 ms, 1000 steps,
+    warm-started PCG per step."""
+    from cudafemproject_gb300 import meshgen
+    from cudafemproject_gb300.meshio import WaveletParams
+    from cudafemproject_gb300.solver import FemContext
+    p = meshgen.box_3d(32, 32, 256, lz=8.0, E=2e7, nu=0.25, rho=2000.0, traction=(0.0, 0.0, 0.0),
+                       point_load=("top_centre", (0.0, 0.0, -1.0)))
+    ctx = FemContext(p, semantics="consistent")
+    X = p.nodes[p.elems]
+    vol = np.abs(np.einsum("ij,ij->i", X[:, 1] - X[:, 0], np.cross(X[:, 2] - X[:, 0], X[:, 3] - X[:, 0]))) / 6
+    m = np.zeros(p.n_nodes)
+    np.add.at(m, p.elems.ravel(), np.repeat(p.rho * vol / 4, 4))
+    minv = np.repeat(1.0 / m, 3)
+    x = np.random.default_rng(5).standard_normal(p.n_dof)
+    lam = 0.0
+    for _ in range(100):
+        y = minv * ctx.matvec(x, "fp64")
+        lam = float(np.linalg.norm(y) / np.linalg.norm(x))
+        x = y / np.linalg.norm(y)
+    dt = 0.5 * 2.0 / np.sqrt(lam)
+    w = WaveletParams("ricker", 25.0, 0.0, 1.0)
+    res = {}
+    for prec in ("fp32", "fp64"):
+        ctx.dyn(0.5, 0.0, dt, 10 * dt * 1.0000001, precision=prec, wavelet=w)
+        u, info = ctx.dyn(0.5, 0.0, dt, 5000 * dt * 1.0000001, precision=prec, wavelet=w)
+        res["explicit_" + prec] = {"steps": info["steps"], "ms": round(info["solve_ms"], 1),
+                                   "steps_per_s": round(info["steps"] / (info["solve_ms"] * 1e-3), 1)}
+    ue32, _ = ctx.dyn(0.5, 0.0, dt, 200 * dt * 1.0000001, precision="fp32", wavelet=w)
+    ue64, _ = ctx.dyn(0.5, 0.0, dt, 200 * dt * 1.0000001, precision="fp64", wavelet=w)
+    res["explicit_fp32_vs_fp64_rel_diff_200_steps"] = float(np.linalg.norm(ue32 - ue64) / np.linalg.norm(ue64))
+    u, info = ctx.dyn(0.5, 0.5, 1e-3, 1000 * 1e-3 * 1.0000001, precision="fp64", wavelet=w, pcg_tol=1e-10,
+                      stop_rule="residual", warm_start=True)
+    res["implicit_fp64"] = {"steps": info["steps"], "ms": round(info["solve_ms"], 1),
+                            "steps_per_s": round(info["steps"] / (info["solve_ms"] * 1e-3), 1),
+                            "pcg_iterations": info["pcg_iterations"]}
+    _line("elastodynamics steps/s (explicit, FP32)", res["explicit_fp32"]["steps_per_s"], "steps/s", True,
+          {"workload": "tet column 1x1x8, 32x32x256 x 6 (1,572,864 tets, 839,619 DOF), Ricker 25 Hz point force",
+           "explicit_dt": dt, "omega_max": float(np.sqrt(lam))}, res)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -149,7 +326,12 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--small", action="store_true", help="a 24x24x96 box (profiling runs)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--workload", default="cantilever", choices=["cantilever", "multi_rhs", "batch", "adjoint", "dynamics"],
+                    help="cantilever: the headline solve; the others measure the remaining configurations "
+                         "(one JSON line each, single GPU)")
     args = ap.parse_args()
+    if args.workload != "cantilever" and args.impl != "reference":
+        return run_other_workload(args)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -87,6 +87,8 @@ SIGNATURES = [
     ("cfem_static_solve", i32, [vp, C.POINTER(Wavelet), C.POINTER(SolveParams), vp, C.POINTER(SolveInfo)]),
     ("cfem_dyn", i32, [vp, C.POINTER(DynParams), C.POINTER(Wavelet), vp, C.POINTER(DynInfo)]),
     ("cfem_pcg_multi", i32, [vp, C.POINTER(SolveParams), i32, vp, vp, C.POINTER(SolveInfo)]),
+    ("cfem_autotune_patch_elems", i32, [C.POINTER(Mesh), C.POINTER(Material), C.POINTER(Options), vp, i32,
+                                        C.POINTER(i32), vp]),
     ("cfem_create_batch", i32, [C.POINTER(vp), i32, C.POINTER(Mesh), C.POINTER(Material), C.POINTER(Options), vp]),
     ("cfem_batch_info", i32, [vp, C.POINTER(i32), vp, vp]),
     ("cfem_batch_static_solve", i32, [vp, C.POINTER(SolveParams), vp, C.POINTER(SolveInfo)]),

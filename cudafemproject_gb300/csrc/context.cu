@@ -1085,6 +1085,41 @@ cfem_status cfem_profile_matvec(cfem_ctx *ctx, int32_t precision, int32_t n_laun
   });
 }
 
+// Elements per CTA patch: every candidate builds the context (renumbering,
+// fans, patch blocks) and times the FP32 PCG-form matvec on the device.
+cfem_status cfem_autotune_patch_elems(const cfem_mesh *mesh, const cfem_material *mat, const cfem_options *opt,
+                                      const int32_t *candidates, int32_t n_candidates, int32_t *best,
+                                      double *ms_per_launch) {
+  return run_guarded([&]() -> cfem_status {
+    if (!mesh || !best) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "null argument"};
+    std::vector<int32_t> cand;
+    if (candidates && n_candidates > 0) cand.assign(candidates, candidates + n_candidates);
+    else if (mesh->dim == 3 && (!opt || opt->matvec_form != CFEM_FORM_GRADIENT)) cand = {192, 384, 576, 768};
+    else cand = {256, 512, 1024};
+    cfem_options o = opt ? *opt : cfem_options{CFEM_COMPAT, CFEM_FORM_AUTO, 0, 0};
+    double best_ms = 1e300;
+    *best = 0;
+    for (size_t i = 0; i < cand.size(); ++i) {
+      if (cand[i] <= 0) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "candidate patch sizes must be positive"};
+      o.patch_elems = cand[i];
+      cfem_ctx *c = nullptr;
+      cfem_status st = cfem_create(&c, mesh, mat, &o, nullptr);
+      if (st != CFEM_OK) return st;
+      double ms = 0, bytes = 0;
+      st = cfem_profile_matvec(c, CFEM_FP32, 3, &ms, &bytes);            // warm-up
+      if (st == CFEM_OK) st = cfem_profile_matvec(c, CFEM_FP32, 20, &ms, &bytes);
+      cfem_destroy(c);
+      if (st != CFEM_OK) return st;
+      if (ms_per_launch) ms_per_launch[i] = ms;
+      if (ms < best_ms) {
+        best_ms = ms;
+        *best = cand[i];
+      }
+    }
+    return CFEM_OK;
+  });
+}
+
 }  // extern "C"
 
 // dynamics, multi-RHS and adjoint entry points live in context_dyn.cu

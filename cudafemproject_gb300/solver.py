@@ -57,6 +57,26 @@ def _mesh_struct(p: Problem):
     return mesh, k
 
 
+def autotune_patch_elems(p: Problem, semantics: str = "compat", matvec_form: str = "auto", candidates=None):
+    """Elements per CTA patch for this mesh on the current GPU
+    (cfem_autotune_patch_elems): returns (best, {candidate: ms per matvec})."""
+    mesh, keep = _mesh_struct(p)
+    mat = capi.Material(float(p.E), float(p.nu), float(p.rho))
+    form = {"gradient": capi.FORM_GRADIENT, "auto": capi.FORM_AUTO, "fan": capi.FORM_GRADIENT_FAN}[matvec_form]
+    opt = capi.Options({"compat": capi.COMPAT, "consistent": capi.CONSISTENT}[semantics], form, 0, 0)
+    cand = None if candidates is None else np.ascontiguousarray(candidates, np.int32)
+    n = 0 if cand is None else len(cand)
+    times = np.zeros(max(n, 4 if p.dim == 3 and matvec_form != "gradient" else 3))
+    best = C.c_int32(0)
+    st = capi.lib().cfem_autotune_patch_elems(C.byref(mesh), C.byref(mat), C.byref(opt),
+                                              None if cand is None else cand.ctypes.data, n, C.byref(best),
+                                              times.ctypes.data)
+    capi.check(st, "cfem_autotune_patch_elems")
+    used = list(cand) if cand is not None else ([192, 384, 576, 768] if p.dim == 3 and matvec_form != "gradient"
+                                                  else [256, 512, 1024])
+    return int(best.value), dict(zip(used, times[:len(used)].tolist()))
+
+
 class FemContext:
     """One mesh on the current GPU. ``semantics`` is "compat" (reproduce the
     reference, quirks included) or "consistent" (textbook operators/loads)."""
@@ -70,6 +90,9 @@ class FemContext:
         self.ndof = p.n_dof
         self.w = 6 * (p.dim - 1)
         L = capi.lib()
+        if patch_elems == "auto":
+            patch_elems, _ = autotune_patch_elems(p, semantics, matvec_form)
+        self.patch_elems = int(patch_elems)
         mesh, self._keep = _mesh_struct(p)
         mat = capi.Material(float(p.E), float(p.nu), float(p.rho))
         form = {"gradient": capi.FORM_GRADIENT, "stored_ke": capi.FORM_STORED_KE, "auto": capi.FORM_AUTO,

@@ -108,7 +108,8 @@ typedef struct cfem_material {
 typedef struct cfem_options {
   int32_t semantics;     /* cfem_semantics */
   int32_t matvec_form;   /* cfem_matvec_form */
-  int32_t patch_elems;   /* elements per CTA patch, 0 = autotuned */
+  int32_t patch_elems;   /* elements per CTA patch, 0 = default (768 for edge fans, 512 per element);
+                            cfem_autotune_patch_elems measures the best value for a mesh */
   int32_t verbose;       /* print PCG scalars like PRINT_DEBUG_INFO */
 } cfem_options;
 
@@ -245,6 +246,16 @@ CFEM_API cfem_status cfem_batch_static_solve(cfem_ctx *ctx, const cfem_solve_par
  * local connectivity, per node z and p read, p written, y accumulated. */
 CFEM_API cfem_status cfem_profile_matvec(cfem_ctx *ctx, int32_t precision, int32_t n_launches, double *ms_per_launch,
                                          double *bytes_per_launch);
+/* Autotuner for the elements per CTA patch (no counterpart in the reference):
+ * builds the mesh's context once per candidate patch size (NULL candidates:
+ * 192, 384, 576, 768 tets for edge fans, 256, 512, 1024 elements otherwise),
+ * times the FP32 PCG-form matvec of each on the current device, and returns
+ * the fastest in *best (pass it as cfem_options.patch_elems).
+ * ms_per_launch: NULL or [n_candidates] measured times. The cases-per-thread
+ * parameter of cfem_pcg_multi is tuned inside that call. */
+CFEM_API cfem_status cfem_autotune_patch_elems(const cfem_mesh *mesh, const cfem_material *mat, const cfem_options *opt,
+                                               const int32_t *candidates, int32_t n_candidates, int32_t *best,
+                                               double *ms_per_launch);
 /* Element strains and stresses of a displacement field u (caller order):
  * strain = B u_e, stress = D_e strain in Voigt order (xx, yy, xy) / (xx, yy, zz,
  * xy, yz, xz), engineering shear; von Mises stress per element

@@ -280,3 +280,18 @@ def test_element_stress_golden(ctxs, name):
     voigt = np.column_stack([g[:, 0], g[:, 4], g[:, 1]])  # xx, yy, xy
     assert rel(sig, voigt) < 2e-5
     assert rel(mis, g[:, 9]) < 2e-5
+
+
+def test_autotune_patch_elems():
+    """The autotuner returns one of its candidates, and a context built with it
+    solves like the default one."""
+    from cudafemproject_gb300.solver import FemContext, autotune_patch_elems
+    p = meshgen.box_3d(8, 8, 24, jitter=0.2, seed=4)
+    best, times = autotune_patch_elems(p, "consistent")
+    assert best in times and all(t > 0 for t in times.values())
+    ctx = FemContext(p, semantics="consistent", patch_elems="auto")
+    assert ctx.patch_elems in times
+    xo, _ = O.Oracle(p, consistent=True).static(tol=1e-14, rule=1)
+    u, _ = ctx.static_solve("fp64", tol=1e-14, stop_rule="residual")
+    assert rel(u, xo) <= 1e-10
+
