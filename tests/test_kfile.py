@@ -1,0 +1,51 @@
+"""LS-DYNA keyword reader (cudafemproject_gb300.kfile) on the CPU: the
+reference's own raw meshes give the committed prepared meshes (made by the
+reference's converter), and a written keyword file reads back."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from cudafemproject_gb300 import kfile, meshgen, meshio
+
+REF_RAW = "/root/reference/raw_meshes/2D"
+
+
+@pytest.mark.parametrize("task", ["test_rect_pcg", "9task_3"])
+def test_reference_raw_meshes_give_the_golden_prepared_meshes(task, tmp_path):
+    raw = os.path.join(REF_RAW, task + ".k")
+    if not os.path.exists(raw):
+        pytest.skip("reference raw meshes not present")
+    kfile.convert(raw, str(tmp_path / task), 2)
+    a = meshio.read_task(str(tmp_path / task), 2)
+    b = meshio.read_task(os.path.join(GOLDEN, "meshes", "2D", task), 2)
+    for f in ("nodes", "elems", "cons", "load_node", "load_vec", "face_nodes", "face_elem", "face_normal",
+              "face_pressure"):
+        assert np.array_equal(getattr(a, f), getattr(b, f)), f
+
+
+def test_keyword_round_trip_3d(tmp_path):
+    p = meshgen.box_3d(3, 2, 5, jitter=0.2, seed=1, traction=(0.0, -1e3, 0.0))
+    path = str(tmp_path / "box.k")
+    kfile.write_k(p, path)
+    q = kfile.read_k(path, 3)
+    assert np.array_equal(q.nodes, p.nodes)
+    assert np.array_equal(q.elems, p.elems)
+    assert np.array_equal(np.sort(q.cons, axis=0), np.sort(p.cons, axis=0))
+    assert np.array_equal(q.face_nodes[:, :3], p.face_nodes[:, :3])
+    assert np.array_equal(q.face_elem, p.face_elem)
+    assert np.array_equal(q.face_nodes[:, 3], p.face_nodes[:, 3])
+    # normals: geometric, pointing away from the element's remaining node
+    for fn, n in zip(q.face_nodes, q.face_normal):
+        x = q.nodes[fn]
+        assert np.dot(n, x[3] - x[0]) < 0
+        assert np.allclose(np.cross(n, np.cross(x[1] - x[0], x[2] - x[0])), 0, atol=1e-12)
+
+
+def test_spc_without_dofs_is_rejected(tmp_path):
+    path = tmp_path / "bad.k"
+    path.write_text("*NODE\n$\n1 0 0\n2 1 0\n3 0 1\n$\n*ELEMENT_SHELL\n1 1 1 2 3 3\n"
+                    "*BOUNDARY_SPC_SET\n1 0 0 0 0\n*SET_NODE_LIST\n1\n1 2\n*END\n")
+    with pytest.raises(ValueError):
+        kfile.read_k(str(path), 2)
