@@ -20,7 +20,7 @@ INC = -I$(REF)/matrix_pack/include -I$(REF)/fem_utils/include \
       -I$(REF)/DataKeeper/src -I$(REF)/femstruct/src -I$(REF)/Tools/src \
       -I$(REF)/VTKfile/src -I$(REF)/femfunc/src \
       -I$(REF)/thirdparty/segyio/include -I$(REF)/thirdparty/json/single_include \
-      -I$(REF)/thirdparty
+      -I$(REF)/thirdparty -I$(REF)/thirdparty/segyio2/include -I$(REF)/segyUtils/src
 
 SRCS = $(REF)/femfunc/src/femfunc.cpp \
        $(REF)/fem_utils/src/fem_utils.cpp \
@@ -33,15 +33,22 @@ SRCS = $(REF)/femfunc/src/femfunc.cpp \
        $(REF)/VTKfile/src/VTKfile.cpp \
        $(REF)/thirdparty/segyio/src/SegyIO.cpp \
        $(REF)/thirdparty/segyio/src/SegyIn.cpp \
-       $(REF)/thirdparty/segyio/src/SegyOut.cpp
+       $(REF)/thirdparty/segyio/src/SegyOut.cpp \
+       $(REF)/segyUtils/src/segyUtils.cpp
+CSRCS = $(REF)/thirdparty/segyio2/src/segy.c
+CC ?= gcc
 
-OBJS = $(patsubst $(REF)/%.cpp,$(OUT)/obj/%.o,$(SRCS))
+OBJS = $(patsubst $(REF)/%.cpp,$(OUT)/obj/%.o,$(SRCS)) $(patsubst $(REF)/%.c,$(OUT)/obj/%.c.o,$(CSRCS))
 
 all: $(OUT)/ref_driver
 
 $(OUT)/obj/%.o: $(REF)/%.cpp
 	@mkdir -p $(dir $@)
 	$(CXX) $(CXXFLAGS) $(INC) -c $< -o $@
+
+$(OUT)/obj/%.c.o: $(REF)/%.c
+	@mkdir -p $(dir $@)
+	$(CC) -O2 -std=gnu99 -w $(INC) -c $< -o $@
 
 $(OUT)/obj/ref_driver.o: oracle/ref_driver.cpp
 	@mkdir -p $(dir $@)

@@ -11,9 +11,12 @@
 //   ref_driver dump   <config.json> <task> <outdir>    setup arrays (mask, adjElements,
 //                                                       Klocals, Flocals, constraints ...)
 //   ref_driver iters  <config.json> <task> <k>         setup time + k timed PCG iterations
+//   ref_driver segy   <out.sgy> <receivers.txt> <nodes.txt> <dim> <dof> <type> <n_elems>
+//                     receiver text file -> SEG-Y by the reference's segyUtils convert()
 //
 // Every mode prints one JSON line on stdout with timings and counters.
 #include <femfunc.h>
+#include <segyUtils.h>
 
 #include <chrono>
 #include <cstdio>
@@ -150,6 +153,20 @@ int main(int argc, char **argv) {
     return 2;
   }
   std::string mode = argv[1];
+  if (mode == "segy" && argc >= 9) {
+    // nodes.txt: the prepared-mesh node file (count, then DIM coordinates per line)
+    std::ifstream nf(argv[4]);
+    size_t n = 0;
+    nf >> n;
+    const int dim = std::atoi(argv[5]);
+    CPU_Matrix nodes(n, dim);
+    for (size_t i = 0; i < n; ++i)
+      for (int d = 0; d < dim; ++d) nf >> nodes(i, d);
+    convert(argv[2], argv[3], (ReceiversType::eType)std::atoi(argv[7]), nodes, std::atoi(argv[6]),
+            std::atoi(argv[8]), n);
+    std::printf("{\"mode\": \"segy\"}\n");
+    return 0;
+  }
   if (mode == "static") return run_solve(false, argv[2], argv[3], argv[4]);
   if (mode == "dyn") return run_solve(true, argv[2], argv[3], argv[4]);
   if (mode == "dump") return run_dump(argv[2], argv[3], argv[4]);

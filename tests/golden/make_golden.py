@@ -12,6 +12,9 @@ the reference checkout; the GPU tests only read the committed outputs).
    is run on those meshes and on small seeded synthetic meshes; its float32
    outputs (static displacements, dynamics displacements and setup arrays)
    are stored as .npz.
+3. A seeded receiver text file and node list are converted to SEG-Y by the
+   reference's segyUtils convert() (``ref_driver segy``); the three files are
+   stored under segy/ (``--only segy`` regenerates just these).
 """
 from __future__ import annotations
 
@@ -78,12 +81,40 @@ def write_cfg(work, dim, E, nu, extra=None):
     return path
 
 
+def make_segy():
+    """Receiver traces with zeros, negative zero and magnitudes 1e-12..1e5 at
+    nodes with negative and almost-integer coordinates; 40 samples of 2.5 ms
+    (interval above 32767 us, so the headers hold ms), velocity along y."""
+    from cudafemproject_gb300 import segy
+    dst = os.path.join(HERE, "segy")
+    os.makedirs(dst, exist_ok=True)
+    rng = np.random.default_rng(11)
+    nodes = (rng.standard_normal((30, 2)) * 40).astype(np.float32)
+    nodes[4] = [2.9999998, -0.75]
+    with open(os.path.join(dst, "nodes.txt"), "w") as f:
+        f.write(f"{len(nodes)}\n")
+        for x in nodes:
+            f.write(" ".join(repr(float(v)) for v in x) + "\n")
+    times = np.arange(1, 41, dtype=np.float32) * np.float32(0.05)
+    tr = (rng.standard_normal((40, 4)) * 10.0 ** rng.integers(-12, 6, (40, 4))).astype(np.float32)
+    tr[0, 0] = 0.0
+    tr[1, 1] = -0.0
+    segy.write_receiver_text(os.path.join(dst, "receivers.txt"), [4, 17, 0, 29], times, tr)
+    subprocess.run([DRIVER, "segy", os.path.join(dst, "reference.sgy"), os.path.join(dst, "receivers.txt"),
+                    os.path.join(dst, "nodes.txt"), "2", "1", str(segy.VELOCITY), "123"], check=True,
+                   capture_output=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", choices=["segy"], default=None)
     args = ap.parse_args()
     if not os.path.exists(DRIVER):
         subprocess.run(["make", "-f", "oracle/ref.mk", f"REF={args.ref}/FEMproject", "-j8"], cwd=REPO, check=True)
+    make_segy()
+    if args.only == "segy":
+        return
     sys.path.insert(0, args.ref)
     from mesh_parser_lib.fem_parser import run_parser  # the reference's own parser
 

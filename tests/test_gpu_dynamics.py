@@ -82,3 +82,20 @@ def test_receiver_traces():
     # the trace of every step equals the final displacement of a shorter run
     u3, _ = ctx.dyn(0.5, 0.0, 1e-5, 3e-5 * 1.0000001, precision="fp64")
     assert rel(tr[2], u3[rec]) < 1e-12
+
+
+def test_receiver_traces_to_segy(tmp_path):
+    from cudafemproject_gb300 import segy
+    from cudafemproject_gb300.solver import FemContext
+    p = meshgen.box_3d(2, 2, 4, rho=2000.0, traction=(0.0, -1e3, 0.0))
+    ctx = FemContext(p)
+    rec = np.array([p.n_nodes - 1, p.n_nodes // 2, 0], np.int32)
+    _, info, tr = ctx.dyn(0.5, 0.0, 1e-5, 2e-4, precision="fp64", receivers=rec)
+    path = str(tmp_path / "rec.sgy")
+    segy.traces_to_segy(path, p.nodes, p.n_elems, rec, 1e-5, tr, dof=1)
+    text, bh, traces = segy.read_segy(path)
+    assert bh["samples"] == info["steps"] and bh["interval"] == 10 and len(traces) == 3
+    for k, (th, s) in enumerate(traces):
+        col = tr[:, k, 1].astype(np.float32).astype(np.float64)
+        assert th["inline"] == rec[k]
+        assert np.all(np.abs(s - col) <= np.abs(col) * 2.0 ** -20)
