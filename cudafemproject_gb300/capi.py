@@ -18,7 +18,7 @@ OK, ERR_INVALID_ARGUMENT, ERR_CUDA, ERR_OUT_OF_MEMORY, ERR_NOT_CONVERGED, ERR_DI
 COMPAT, CONSISTENT = 0, 1
 FP64, FP32, FP32_REFINE = 0, 1, 2
 STOP_REFERENCE, STOP_RESIDUAL = 0, 1
-FORM_AUTO, FORM_GRADIENT, FORM_STORED_KE, FORM_GRADIENT_FAN = 0, 1, 2, 3
+FORM_AUTO, FORM_GRADIENT, FORM_STORED_KE, FORM_GRADIENT_FAN, FORM_GEOMETRY_FAN = 0, 1, 2, 3, 4
 
 STATUS_NAMES = {0: "CFEM_OK", 1: "CFEM_ERR_INVALID_ARGUMENT", 2: "CFEM_ERR_CUDA", 3: "CFEM_ERR_OUT_OF_MEMORY",
                 4: "CFEM_ERR_NOT_CONVERGED", 5: "CFEM_ERR_DIVERGED", 6: "CFEM_ERR_MESH", 7: "CFEM_ERR_UNSUPPORTED",

@@ -54,6 +54,17 @@ void launch_mv_t(cfem_ctx *c, int mode, const MvParams<T> &P) {
       F.fan_off = c->fan_off.p;
       F.fan_elem_off = c->fan_elem_off.p;
       F.err = c->tma_err.p;
+      if (c->geo && !P.patch_inst) {
+        F.blocks = c->blkg.p;
+        F.L = c->Lg;
+        dim3 g(c->grid_geo), b(kHfanThreads);
+        if (mode == MV_PLAIN) k_matvec_fan_tma<float, MV_PLAIN, true><<<g, b, c->smem_geo, c->stream>>>(P, F);
+        else if (mode == MV_PCG) k_matvec_fan_tma<float, MV_PCG, true><<<g, b, c->smem_geo, c->stream>>>(P, F);
+        else k_matvec_fan_tma<float, MV_DYN, true><<<g, b, c->smem_geo, c->stream>>>(P, F);
+        CKL();
+        c->launches += 1;
+        return;
+      }
       dim3 g(c->grid_ft32), b(kHfanThreads);
       if (mode == MV_PLAIN) k_matvec_fan_tma<float, MV_PLAIN><<<g, b, c->smem_ft32, c->stream>>>(P, F);
       else if (mode == MV_PCG) k_matvec_fan_tma<float, MV_PCG><<<g, b, c->smem_ft32, c->stream>>>(P, F);
@@ -384,12 +395,13 @@ void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, co
   const int req_form = opt ? opt->matvec_form : CFEM_FORM_AUTO;
   if (req_form == CFEM_FORM_STORED_KE)
     throw Fail{CFEM_ERR_UNSUPPORTED, "stored K_e form is not built in this library version"};
-  if (req_form < CFEM_FORM_AUTO || req_form > CFEM_FORM_GRADIENT_FAN)
+  if (req_form < CFEM_FORM_AUTO || req_form > CFEM_FORM_GEOMETRY_FAN)
     throw Fail{CFEM_ERR_INVALID_ARGUMENT, "unknown matvec_form"};
-  if (req_form == CFEM_FORM_GRADIENT_FAN && m->dim != 3)
-    throw Fail{CFEM_ERR_INVALID_ARGUMENT, "the edge-fan form is for tetrahedra (dim 3)"};
-  c->fans = m->dim == 3 && (req_form == CFEM_FORM_AUTO || req_form == CFEM_FORM_GRADIENT_FAN);
-  c->form = c->fans ? CFEM_FORM_GRADIENT_FAN : CFEM_FORM_GRADIENT;
+  if ((req_form == CFEM_FORM_GRADIENT_FAN || req_form == CFEM_FORM_GEOMETRY_FAN) && m->dim != 3)
+    throw Fail{CFEM_ERR_INVALID_ARGUMENT, "the edge-fan forms are for tetrahedra (dim 3)"};
+  c->fans = m->dim == 3 && req_form != CFEM_FORM_GRADIENT;
+  c->geo = c->fans && req_form == CFEM_FORM_GEOMETRY_FAN;
+  c->form = c->geo ? CFEM_FORM_GEOMETRY_FAN : c->fans ? CFEM_FORM_GRADIENT_FAN : CFEM_FORM_GRADIENT;
   c->verbose = opt ? opt->verbose : 0;
   c->E = mat ? mat->young_modulus : 2e7;
   c->nu = mat ? mat->poisson_ratio : 0.3;
@@ -466,6 +478,11 @@ void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, co
       uint8_t *bt = B + c->L32.bits_off;
       const int f0 = P.p_fan_off[p], nf = P.p_fan_off[p + 1] - f0;
       const int nb = P.p_node_off[p], n = P.p_node_off[p + 1] - nb;
+      int32_t *hdr = reinterpret_cast<int32_t *>(B + c->L32.hdr_off);
+      hdr[0] = n;
+      hdr[1] = P.p_own[p];
+      hdr[2] = nf;
+      hdr[3] = 0;
       for (int fl = 0; fl < nf; ++fl)
         for (int k = 0; k < kFanSlots; ++k) sl[k * kFanThreads + fl] = P.fan_slot[(size_t)(f0 + fl) * kFanSlots + k];
       // half-fan incidences (fan fl, half h, slot hs), counting-sorted by node
@@ -631,9 +648,25 @@ void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, co
       CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o32, k_matvec_fan_tma<float, MV_PCG>, kHfanThreads, c->smem_ft32));
       c->grid_ft32 = (int)std::min<int64_t>(P.n_patches, (int64_t)c->n_sm * std::max(o32, 1));
     }
+    if (c->geo && !c->fan_tma) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "fan patch too large for shared memory: lower patch_elems"};
+    if (c->geo) {
+      // the largest layout (with scale rows) bounds the shared memory of every later rebuild
+      const size_t smem_max = fan_tma_smem_bytes(fan_geo_block_layout(P.np_max, true), sizeof(float));
+      for (const void *k : {(const void *)k_matvec_fan_tma<float, MV_PLAIN, true>,
+                            (const void *)k_matvec_fan_tma<float, MV_PCG, true>,
+                            (const void *)k_matvec_fan_tma<float, MV_DYN, true>})
+        CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max));
+    }
   }
   c->grid_vec = (int)std::min<int64_t>(std::max<int64_t>(1, nblk(c->nn)), (int64_t)c->n_sm * 4);
-  int maxgrid = std::max({c->grid_mv, c->grid_vec, c->grid_fan, c->grid_ft32});
+  if (c->geo) {  // the grid of the largest geometry layout fits every later one
+    int og = 1;
+    const size_t smem_max = fan_tma_smem_bytes(fan_geo_block_layout(P.np_max, true), sizeof(float));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&og, k_matvec_fan_tma<float, MV_PCG, true>, kHfanThreads,
+                                                     smem_max));
+    c->grid_geo = (int)std::min<int64_t>(P.n_patches, (int64_t)c->n_sm * std::max(og, 1));
+  }
+  int maxgrid = std::max({c->grid_mv, c->grid_vec, c->grid_fan, c->grid_ft32, c->grid_geo});
   c->partials.alloc((size_t)maxgrid * 4);
   c->counters.alloc(4);
   c->counters.zero(s);
@@ -645,6 +678,28 @@ void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, co
   CK(cudaEventCreate(&c->ev0));
   CK(cudaEventCreate(&c->ev1));
   CK(cudaStreamSynchronize(s));
+}
+
+// Geometry blocks from the gradient blocks' prefix (slot .. bits), the
+// patch-relative coordinates and, with per-element moduli, the scale rows.
+static void build_geo_blocks(cfem_ctx *c) {
+  cudaStream_t s = c->stream;
+  const Prep &P = c->prep;
+  const bool with_scale = !c->young.empty();
+  const FanBlockLayout L = fan_geo_block_layout(P.np_max, with_scale);
+  if (!c->blkg.p || L.bytes != c->Lg.bytes || L.c_off != c->Lg.c_off) c->blkg.alloc((size_t)L.bytes * P.n_patches);
+  c->Lg = L;
+  c->blkg.zero(s);
+  CK(cudaMemcpy2DAsync(c->blkg.p, L.bytes, c->blk32.p, c->L32.bytes, (size_t)c->L32.g_off, P.n_patches,
+                       cudaMemcpyDeviceToDevice, s));
+  k_fan_block_coords<<<P.n_patches, 128, 0, s>>>(c->node_off.p, c->nodes.p, c->coords.p, c->blkg.p, L);
+  CKL();
+  if (with_scale) {
+    k_fan_block_scales<<<nblk(c->ne), kThreads, 0, s>>>(c->ne, c->escale.p, c->fan_pos.p, c->fan_patch.p, c->fan_off.p,
+                                                        c->blkg.p, L);
+    CKL();
+  }
+  c->smem_geo = fan_tma_smem_bytes(L, sizeof(float));
 }
 
 // (Re)builds the element operator: scaled gradients, volumes, assembled
@@ -719,6 +774,7 @@ void rebuild_operator(cfem_ctx *c) {
     k_fan_block_gradients<<<nblk(c->ne), kThreads, 0, s>>>(c->ne, c->G64.p, c->gstride, c->fan_pos.p, c->fan_perm.p,
                                                            c->fan_patch.p, c->fan_off.p, c->blk32.p, c->L32);
     CKL();
+    if (c->geo) build_geo_blocks(c);
   }
   // consistent-mass diagonal: 2 * cons_c * rho * V per DOF, assembled = mlump * 2 cons_c / lump_c
   k_axpby64<<<nblk(c->nvec), kThreads, 0, s>>>(c->nvec, 2 * cons_c / lump_c, c->mlump.p, 0.0, c->mcdiag.p);
@@ -1076,8 +1132,14 @@ cfem_status cfem_profile_matvec(cfem_ctx *ctx, int32_t precision, int32_t n_laun
     float ms = 0;
     CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
     if (ms_per_launch) *ms_per_launch = ms / n_launches;
+    // algorithmic bytes: the operator (stored gradients + 8 bytes of connectivity
+    // per element; geometry form: the streamed patch blocks, which hold the
+    // connectivity, scatter tables and coordinates) and four node-vector streams
     if (bytes_per_launch)
-      *bytes_per_launch = (double)ctx->ne * (ctx->ncomp * ts + 8) + (double)ctx->nn * ctx->vw * ts * 4;
+      *bytes_per_launch = (ctx->geo && precision == CFEM_FP32
+                               ? (double)ctx->prep.n_patches * ctx->Lg.bytes
+                               : (double)ctx->ne * (ctx->ncomp * ts + 8)) +
+                          (double)ctx->nn * ctx->vw * ts * 4;
     // leave the work vectors clean for the next solve
     if (precision == CFEM_FP64) ctx->v64.u.zero(ctx->stream); else ctx->v32.u.zero(ctx->stream);
     check_copy_error(ctx);

@@ -581,6 +581,9 @@ cfem_status cfem_set_young(cfem_ctx *ctx, const double *elem_young) {
       if (!(y > 0)) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "per-element Young's modulus must be positive"};
     ctx->young = yv;
     rebuild_operator(ctx);
+    // captured PCG iterations hold operator buffers that the rebuild may have replaced
+    ctx->graph64.reset();
+    ctx->graph32.reset();
     return CFEM_OK;
   });
 }

@@ -133,6 +133,13 @@ struct cfem_ctx {
   int *h_tma_err = nullptr;
   size_t smem_ft32 = 0;
   int grid_ft32 = 0;
+  // geometry blocks (FP32 single-RHS matvec of CFEM_FORM_GEOMETRY_FAN): the
+  // prefix of blk32, then patch-relative coordinates and per-tet moduli scales
+  bool geo = false;
+  FanBlockLayout Lg{};
+  DBuf<unsigned char> blkg;
+  size_t smem_geo = 0;
+  int grid_geo = 0;
   int np_slots = 0;               // node slots per patch in shared memory
   DBuf<uint8_t> bits;
   DBuf<double> coords, escale, young_d;

@@ -3,6 +3,7 @@
 // the six node slots P, Q, R_3h .. R_3h+3 (kHalfSlots = 12 force slots per fan).
 // Everything a patch needs apart from the node vectors lives in one
 // contiguous, 128-byte aligned block of the "patch block" array:
+//   [header: 4 i32]                        patch nodes, first owned node, fans, 0
 //   [slot: kFanSlots x kFanThreads u16]   patch-local nodes P, Q, R_0.. of each fan, then its length
 //   [fpos: kHalfSlots x kFanThreads u16]  position of each (fan, half slot) force in the node-sorted list
 //   [fstart: nps u16]                      node i sums forces fstart[i] .. fstart[i+1]-1
@@ -12,6 +13,13 @@
 // operator stream overlaps the arithmetic of the current patch. The forces of
 // a patch are written into the G region of its own buffer once every thread
 // has read its gradients, and the node sums read them back contiguously.
+//
+// Geometry blocks (GEO) replace the 54 gradient rows by the patch nodes'
+// coordinates relative to the patch's first node, FP32 float4 (16 bytes per
+// patch node instead of 36 bytes per tet), and optionally a per-tet
+// sqrt(E_e / E) row block [kFanMax x kFanThreads]. The gradients are formed
+// from the coordinates in registers (G_b = sqrt(V_e E_e / E) grad N_b from the
+// cofactors of the edge matrix), and the forces go to a separate shared region.
 #pragma once
 
 #include "kernels.cuh"
@@ -33,7 +41,9 @@ __host__ __device__ __forceinline__ int half_slot_count(int h, int len) {
 
 struct FanBlockLayout {
   int bytes;        // per patch, multiple of 128
-  int slot_off, fpos_off, fstart_off, nodes_off, bits_off, g_off;
+  int hdr_off, slot_off, fpos_off, fstart_off, nodes_off, bits_off;
+  int g_off;        // gradient blocks: G rows; geometry blocks: end of the shared prefix
+  int x_off, c_off; // geometry blocks: coordinates, per-tet scale rows (-1: none); else -1
   int nps, npn;     // fstart entries, node entries per patch
 };
 
@@ -43,6 +53,7 @@ inline FanBlockLayout fan_block_layout(int np_max, size_t tsize) {
   L.nps = up(np_max + 1, 8);
   L.npn = up(np_max, 4);
   int off = 0;
+  L.hdr_off = off; off += 16;
   L.slot_off = off; off += kFanSlots * kFanThreads * 2;
   L.fpos_off = off; off += kHalfSlots * kFanThreads * 2;
   L.fstart_off = off; off += L.nps * 2;
@@ -50,11 +61,57 @@ inline FanBlockLayout fan_block_layout(int np_max, size_t tsize) {
   L.bits_off = off; off += up(L.npn, 16);
   L.g_off = up(off, 128);
   L.bytes = up(L.g_off + (int)(kFanMax * 9 * kFanThreads * tsize), 128);
+  L.x_off = L.c_off = -1;
   return L;
 }
 
+// Geometry block: the same prefix (header .. bits), then coordinates and, with
+// per-element moduli, the scale rows.
+inline FanBlockLayout fan_geo_block_layout(int np_max, bool with_scale) {
+  FanBlockLayout L = fan_block_layout(np_max, sizeof(float));
+  int off = L.g_off;
+  L.x_off = off; off += L.npn * 16;
+  L.c_off = -1;
+  if (with_scale) { L.c_off = off; off += kFanMax * kFanThreads * 4; }
+  L.bytes = (off + 127) / 128 * 128;
+  return L;
+}
+
+constexpr int kForceBytes = kHalfSlots * kFanThreads * 16;  // separate force list of geometry blocks
+
+// Geometry blocks: two buffers, the force list, and two stages of the node
+// vectors a PCG-form matvec reads (z and p_old), gathered one patch ahead.
+// Gradient blocks: two buffers and the staged node values.
 inline size_t fan_tma_smem_bytes(const FanBlockLayout &L, size_t tsize) {
+  if (L.x_off >= 0) return (size_t)2 * L.bytes + kForceBytes + (size_t)4 * L.npn * 4 * tsize + 16;
   return (size_t)2 * L.bytes + (size_t)L.npn * 4 * tsize + 16;
+}
+
+// Scaled gradients of the fan tet (P, Q, R_j, R_j+1) from the edge vectors
+// a = x_Q - x_P, b = x_Rj - x_P, c = x_Rj+1 - x_P: grad N_Q = (b x c) / det,
+// grad N_Rj = (c x a) / det, grad N_Rj+1 = (a x b) / det with det = a . (b x c),
+// scaled by sqrt(V sc^2), V = |det| / 6: G = cof * sign(det) * sc / sqrt(6 |det|).
+// Tets that do not exist (valid false) get zero gradients.
+__device__ __forceinline__ void geo_gradients(const float (&a)[3], const float (&b)[3], const float (&c)[3], float sc,
+                                              bool valid, float (&G)[9]) {
+  float c1[3], c2[3], c3[3];
+  c1[0] = b[1] * c[2] - b[2] * c[1];
+  c1[1] = b[2] * c[0] - b[0] * c[2];
+  c1[2] = b[0] * c[1] - b[1] * c[0];
+  c2[0] = c[1] * a[2] - c[2] * a[1];
+  c2[1] = c[2] * a[0] - c[0] * a[2];
+  c2[2] = c[0] * a[1] - c[1] * a[0];
+  c3[0] = a[1] * b[2] - a[2] * b[1];
+  c3[1] = a[2] * b[0] - a[0] * b[2];
+  c3[2] = a[0] * b[1] - a[1] * b[0];
+  const float det = a[0] * c1[0] + a[1] * c1[1] + a[2] * c1[2];
+  const float s = valid ? copysignf(rsqrtf(6.0f * fabsf(det)), det) * sc : 0.0f;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    G[d] = c1[d] * s;
+    G[3 + d] = c2[d] * s;
+    G[6 + d] = c3[d] * s;
+  }
 }
 
 struct FanTmaParams {
@@ -65,15 +122,24 @@ struct FanTmaParams {
   int *err;                     // kErrTmaTimeout on a copy that never completed
 };
 
-template <typename T, int MODE>
+template <typename T, int MODE, bool GEO = false>
 // (3 CTAs per SM: the shared memory of a CTA allows 3, the register bound makes them fit)
 __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> P, FanTmaParams F) {
+  static_assert(!GEO || sizeof(T) == 4, "geometry blocks are FP32");
   constexpr int DIM = 3, VW = 4;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const FanBlockLayout &L = F.L;
   unsigned char *buf0 = smem_raw, *buf1 = smem_raw + L.bytes;
-  T *sp = reinterpret_cast<T *>(smem_raw + 2 * (size_t)L.bytes);  // [npn][4] staged node values
-  uint64_t *bar = reinterpret_cast<uint64_t *>(sp + (size_t)L.npn * VW);
+  unsigned char *tail = smem_raw + 2 * (size_t)L.bytes;
+  T *fgeo = reinterpret_cast<T *>(tail);                          // GEO: [kHalfSlots x kFanThreads][4] forces
+  if (GEO) tail += kForceBytes;
+  T *sp = reinterpret_cast<T *>(tail);                            // [npn][4] staged node values
+  // GEO: [2 stages][z, p_old][npn][4] (PCG form; the other modes use stage 0 as sp)
+  uint64_t *bar = reinterpret_cast<uint64_t *>(sp + (size_t)(GEO ? 4 : 1) * L.npn * VW);
+  // PCG-form geometry kernel: the node vectors of the next patch are gathered
+  // by cp.async while the current one finishes, so their latency is hidden
+  constexpr bool PREFETCH = GEO && MODE == MV_PCG;
+  const int stage_stride = 2 * L.npn * VW;
   const bool batch = P.patch_inst != nullptr;
   if (MODE == MV_PCG && (batch ? P.bctl->all_done : P.sc->done)) return;
   T beta = 0;
@@ -95,6 +161,20 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
       }
     }
   }
+  // gathers of the node vectors of the patch in buffer Bq into stage st
+  auto issue_gathers = [&](const unsigned char *Bq, T *st) {
+    const int32_t *nq = reinterpret_cast<const int32_t *>(Bq + L.nodes_off);
+    const int nnq = reinterpret_cast<const int32_t *>(Bq + L.hdr_off)[0];
+    for (int i = threadIdx.x; i < nnq; i += kHfanThreads) {
+      const int64_t g = nq[i];
+      cp_async16(st + (size_t)i * VW, P.x + g * VW);
+      if (beta != T(0)) cp_async16(st + (size_t)(L.npn + i) * VW, P.x2 + g * VW);
+    }
+  };
+  if constexpr (PREFETCH) {
+    if (blockIdx.x < P.n_patches && mbar_wait_bounded(&bar[0], 0u)) issue_gathers(buf0, sp);
+    cp_async_commit();
+  }
   DotAcc<T> energy;
   int it = 0;
   for (int patch = blockIdx.x; patch < P.n_patches; patch += step, ++it) {
@@ -102,6 +182,7 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
     unsigned char *B = b ? buf1 : buf0;
     const bool ok = mbar_wait_bounded(&bar[b], (unsigned)((it >> 1) & 1));
     if (__syncthreads_or(!ok)) {
+      if (PREFETCH) cp_async_wait<0>();
       if (threadIdx.x == 0) {
         atomicOr(F.err, kErrTmaTimeout);
         if (patch + step < P.n_patches) mbar_wait_bounded(&bar[b ^ 1], (unsigned)(((it + 1) >> 1) & 1));
@@ -113,9 +194,8 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
     const uint16_t *fstart = reinterpret_cast<const uint16_t *>(B + L.fstart_off);
     const int32_t *nodes = reinterpret_cast<const int32_t *>(B + L.nodes_off);
     const uint8_t *bits = B + L.bits_off;
-    const T *Gs = reinterpret_cast<const T *>(B + L.g_off);
-    const int nn = P.node_off[patch + 1] - P.node_off[patch], own = P.own[patch];
-    const int nf = F.fan_off[patch + 1] - F.fan_off[patch];
+    const int32_t *hdr = reinterpret_cast<const int32_t *>(B + L.hdr_off);
+    const int nn = hdr[0], own = hdr[1], nf = hdr[2];
     bool skip = false;
     if (batch) {  // the patch's instance: material, direction update, convergence mask
       lam = P.pmat[2 * patch];
@@ -127,6 +207,28 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
       }
     }
     if (!skip) {
+    T *spp = sp;  // staged node values of this patch
+    if constexpr (PREFETCH) {
+      // 1. the gathered z and p_old of this patch: p = z + beta p_old, owned
+      //    nodes written out, constrained DOFs masked, in place
+      cp_async_wait<0>();
+      __syncthreads();
+      spp = sp + (size_t)(it & 1) * stage_stride;
+      for (int i = threadIdx.x; i < nn; i += kHfanThreads) {
+        NodeV<T, VW> v = ldv<T, VW>(spp, i);
+        if (beta != T(0)) {
+          const NodeV<T, VW> w = ldv<T, VW>(spp + (size_t)L.npn * VW, i);
+#pragma unroll
+          for (int d = 0; d < DIM; ++d) v.v[d] += beta * w.v[d];
+        }
+        if (i >= own) stv<T, VW>(P.xout, nodes[i], v);
+        const unsigned bb = bits[i];
+        NodeV<T, VW> m;
+#pragma unroll
+        for (int d = 0; d < VW; ++d) m.v[d] = (d < DIM && !(bb >> d & 1u)) ? v.v[d] : T(0);
+        stv<T, VW>(spp, i, m);
+      }
+    } else {
     // 1. stage node values: each thread issues the gathers of all its nodes
     //    (up to kStageUnroll) before using any of them
     constexpr int SU = kStageUnroll;
@@ -165,41 +267,64 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
         stv<T, VW>(sp, i, m);
       }
     }
+    }  // PREFETCH
     __syncthreads();
     // 2. half a fan per thread (tets 3h .. 3h+2), forces kept in registers.
-    //    Missing tets have zero gradients in the block, so the three tets are
-    //    straight-line code; differences to P are formed once per node slot.
+    //    Missing tets have zero gradients, so the three tets are straight-line
+    //    code; differences to P are formed once per node slot.
     const int fl = threadIdx.x >> 1, h = threadIdx.x & 1;
     const int len = fl < nf ? sl[(kFanSlots - 1) * kFanThreads + fl] : 0;
     const int nk = half_slot_count(h, len);
     T fv[6][DIM];
     {
-      T uv[6][DIM];
+      T du[6][DIM];  // node values of the slots (differences to P after step a)
+      T dx[6][DIM];  // GEO: coordinates of the slots relative to P
+      const float *Xs = reinterpret_cast<const float *>(B + (GEO ? L.x_off : 0));
 #pragma unroll
       for (int k = 0; k < 6; ++k) {
-        NodeV<T, VW> s;
+        NodeV<T, VW> s, xk;
 #pragma unroll
-        for (int d = 0; d < VW; ++d) s.v[d] = 0;
-        if (k < nk) s = ldv<T, VW>(sp, sl[half_slot_to_fan(h, k) * kFanThreads + fl]);
+        for (int d = 0; d < VW; ++d) s.v[d] = xk.v[d] = 0;
+        if (k < nk) {
+          const int slot = sl[half_slot_to_fan(h, k) * kFanThreads + fl];
+          s = ldv<T, VW>(spp, slot);
+          if (GEO) xk = ldv<T, VW>(reinterpret_cast<const T *>(Xs), slot);
+        }
 #pragma unroll
         for (int d = 0; d < DIM; ++d) {
-          uv[k][d] = s.v[d];
+          du[k][d] = s.v[d];
+          dx[k][d] = xk.v[d];
           fv[k][d] = 0;
         }
       }
-      if (P.mcoef == nullptr) {
-        const T lamk = lam * P.cK, muk = mu * P.cK;
-        T du[6][DIM];
+      if (GEO) {
 #pragma unroll
         for (int k = 1; k < 6; ++k)
 #pragma unroll
-          for (int d = 0; d < DIM; ++d) du[k][d] = uv[k][d] - uv[0][d];
-#pragma unroll
-        for (int jj = 0; jj < 3; ++jj) {
-          const int j = 3 * h + jj;
-          T G[9];
+          for (int d = 0; d < DIM; ++d) dx[k][d] -= dx[0][d];
+      }
+      // gradients of tet jj of this half: from the block, or from the coordinates
+      auto tet_G = [&](int jj, T (&G)[9]) {
+        const int j = 3 * h + jj;
+        if constexpr (GEO) {
+          const float sc = L.c_off >= 0 ? reinterpret_cast<const float *>(B + L.c_off)[j * kFanThreads + fl] : 1.0f;
+          geo_gradients(dx[1], dx[2 + jj], dx[3 + jj], sc, j < len, G);
+        } else {
+          const T *Gs = reinterpret_cast<const T *>(B + L.g_off);
 #pragma unroll
           for (int k = 0; k < 9; ++k) G[k] = Gs[(j * 9 + k) * kFanThreads + fl];
+        }
+      };
+      if (P.mcoef == nullptr) {
+        const T lamk = lam * P.cK, muk = mu * P.cK;
+#pragma unroll
+        for (int k = 1; k < 6; ++k)
+#pragma unroll
+          for (int d = 0; d < DIM; ++d) du[k][d] -= du[0][d];
+#pragma unroll
+        for (int jj = 0; jj < 3; ++jj) {
+          T G[9];
+          tet_G(jj, G);
           T f1[3], f2[3], f3[3];
           tet_forces_rel<T>(du[1], du[2 + jj], du[3 + jj], G, lamk, muk, f1, f2, f3);
 #pragma unroll
@@ -211,6 +336,14 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
         }
 #pragma unroll
         for (int d = 0; d < DIM; ++d) fv[0][d] = -(fv[1][d] + fv[2][d] + fv[3][d] + fv[4][d] + fv[5][d]);
+        if (MODE == MV_PCG) {  // p.Ap of this half-fan: the forces sum to zero, so sum_k u_k.f_k = sum_k>0 du_k.f_k
+          T e_fan = 0;
+#pragma unroll
+          for (int k = 1; k < 6; ++k)
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) e_fan += du[k][d] * fv[k][d];
+          energy.add(e_fan);
+        }
       } else {  // consistent mass term: forces do not sum to zero per tet
         const int64_t fe0 = nk ? F.fan_elem_off[F.fan_off[patch] + fl] : 0;
 #pragma unroll
@@ -218,15 +351,14 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
           const int j = 3 * h + jj;
           if (nk && j < len) {
             T G[9];
-#pragma unroll
-            for (int k = 0; k < 9; ++k) G[k] = Gs[(j * 9 + k) * kFanThreads + fl];
+            tet_G(jj, G);
             T u[4][DIM], fe[4][DIM];
 #pragma unroll
             for (int d = 0; d < DIM; ++d) {
-              u[0][d] = uv[0][d];
-              u[1][d] = uv[1][d];
-              u[2][d] = uv[2 + jj][d];
-              u[3][d] = uv[3 + jj][d];
+              u[0][d] = du[0][d];
+              u[1][d] = du[1][d];
+              u[2][d] = du[2 + jj][d];
+              u[3][d] = du[3 + jj][d];
             }
             element_force<T, DIM>(u, G, P.lam, P.mu, P.cK, P.cM * P.mcoef[fe0 + j], fe);
 #pragma unroll
@@ -238,18 +370,20 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
             }
           }
         }
-      }
-      if (MODE == MV_PCG) {  // p.Ap of this half-fan: sum over its node slots of u . f
-        T e_fan = 0;
+        if (MODE == MV_PCG) {
+          T e_fan = 0;
 #pragma unroll
-        for (int k = 0; k < 6; ++k)
+          for (int k = 0; k < 6; ++k)
 #pragma unroll
-          for (int d = 0; d < DIM; ++d) e_fan += uv[k][d] * fv[k][d];
-        energy.add(e_fan);
+            for (int d = 0; d < DIM; ++d) e_fan += du[k][d] * fv[k][d];
+          energy.add(e_fan);
+        }
       }
     }
-    __syncthreads();  // every thread has read its gradients: the G region becomes the force list
-    T *fs = reinterpret_cast<T *>(B + L.g_off);
+    // the force list: the consumed G region of the buffer once every thread has
+    // read its gradients, or (GEO) the separate force region
+    if (!GEO) __syncthreads();
+    T *fs = GEO ? fgeo : reinterpret_cast<T *>(B + L.g_off);
 #pragma unroll
     for (int k = 0; k < 6; ++k)
       if (k < nk) {
@@ -258,23 +392,29 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
         for (int d = 0; d < VW; ++d) o.v[d] = d < DIM ? fv[k][d] : T(0);
         stv<T, VW>(fs, fpos[(h * 6 + k) * kFanThreads + fl], o);
       }
+    if constexpr (PREFETCH) {  // the next patch's gathers overlap the node sums below
+      if (patch + step < P.n_patches &&
+          mbar_wait_bounded(&bar[b ^ 1], (unsigned)(((it + 1) >> 1) & 1)))
+        issue_gathers(b ? buf0 : buf1, sp + (size_t)((it + 1) & 1) * stage_stride);
+      cp_async_commit();
+    }
     __syncthreads();
     // 3. node sums over contiguous force runs
     for (int i = threadIdx.x; i < nn; i += kHfanThreads) {
       const int g = nodes[i];
       const unsigned bb = bits[i];
-      T acc[DIM] = {0, 0, 0};
+      T acc3[DIM] = {0, 0, 0};
       const int k1 = fstart[i + 1];
       for (int k = fstart[i]; k < k1; ++k) {
         const NodeV<T, VW> fo = ldv<T, VW>(fs, k);
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) acc[d] += fo.v[d];
+        for (int d = 0; d < DIM; ++d) acc3[d] += fo.v[d];
       }
       NodeV<T, VW> r;
       bool any = false;
 #pragma unroll
       for (int d = 0; d < VW; ++d) {
-        T val = (d < DIM && !(bb >> d & 1u)) ? acc[d < DIM ? d : 0] : T(0);
+        T val = (d < DIM && !(bb >> d & 1u)) ? acc3[d < DIM ? d : 0] : T(0);
         r.v[d] = val;
         any |= val != T(0);
       }
@@ -344,6 +484,38 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
     }
     if (threadIdx.x == 0) P.bctl->count_mv = 0;
   }
+}
+
+// Coordinates of the patch nodes relative to the patch's first node, FP32,
+// into the geometry blocks (one CTA per patch; padding slots repeat node 0).
+static __global__ void k_fan_block_coords(const int32_t *node_off, const int32_t *nodes, const double *coords,
+                                          unsigned char *blkg, FanBlockLayout L) {
+  const int p = blockIdx.x;
+  const int base = node_off[p], n = node_off[p + 1] - base;
+  const int g0 = nodes[base];
+  float4 *X = reinterpret_cast<float4 *>(blkg + (size_t)p * L.bytes + L.x_off);
+  for (int i = threadIdx.x; i < L.npn; i += blockDim.x) {
+    const int g = i < n ? nodes[base + i] : g0;
+    float4 v;
+    v.x = (float)(coords[(size_t)g * 3 + 0] - coords[(size_t)g0 * 3 + 0]);
+    v.y = (float)(coords[(size_t)g * 3 + 1] - coords[(size_t)g0 * 3 + 1]);
+    v.z = (float)(coords[(size_t)g * 3 + 2] - coords[(size_t)g0 * 3 + 2]);
+    v.w = 0.0f;
+    X[i] = v;
+  }
+}
+
+// sqrt(E_e / E) of every tet into the scale rows of the geometry blocks.
+static __global__ void k_fan_block_scales(int64_t ne, const double *escale, const int32_t *fan_pos,
+                                          const int32_t *fan_patch, const int32_t *fan_off, unsigned char *blkg,
+                                          FanBlockLayout L) {
+  int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  const int fp = fan_pos[e];
+  const int f = fp >> 3, j = fp & 7;
+  const int p = fan_patch[f];
+  float *C = reinterpret_cast<float *>(blkg + (size_t)p * L.bytes + L.c_off);
+  C[j * kFanThreads + (f - fan_off[p])] = (float)sqrt(escale[e]);
 }
 
 // Scaled gradients into the G part of the FP32 patch blocks from the

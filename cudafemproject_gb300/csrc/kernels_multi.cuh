@@ -93,8 +93,8 @@ __global__ void __launch_bounds__(kHfanThreads) k_matvec_multi(MultiParams<float
       if (threadIdx.x == 0) atomicOr(P.F.err, kErrTmaTimeout);
       return;
     }
-    const int nn = P.node_off[patch + 1] - P.node_off[patch], own = P.own[patch];
-    const int nf = P.F.fan_off[patch + 1] - P.F.fan_off[patch];
+    const int32_t *hdr = reinterpret_cast<const int32_t *>(B + L.hdr_off);
+    const int nn = hdr[0], own = hdr[1], nf = hdr[2];
     const int fl = threadIdx.x >> 1, h = threadIdx.x & 1;
     const int len = fl < nf ? sl[(kFanSlots - 1) * kFanThreads + fl] : 0;
     const int nk = half_slot_count(h, len);

@@ -32,6 +32,15 @@ __device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned b
                : "memory");
 }
 
+// 16-byte asynchronous copy global -> shared (L2 only), completed by cp_async_wait.
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// waits until at most N of this thread's committed groups are still in flight
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
   uint32_t ok;
   asm volatile(

@@ -62,7 +62,8 @@ def autotune_patch_elems(p: Problem, semantics: str = "compat", matvec_form: str
     (cfem_autotune_patch_elems): returns (best, {candidate: ms per matvec})."""
     mesh, keep = _mesh_struct(p)
     mat = capi.Material(float(p.E), float(p.nu), float(p.rho))
-    form = {"gradient": capi.FORM_GRADIENT, "auto": capi.FORM_AUTO, "fan": capi.FORM_GRADIENT_FAN}[matvec_form]
+    form = {"gradient": capi.FORM_GRADIENT, "auto": capi.FORM_AUTO, "fan": capi.FORM_GRADIENT_FAN,
+            "geometry": capi.FORM_GEOMETRY_FAN}[matvec_form]
     opt = capi.Options({"compat": capi.COMPAT, "consistent": capi.CONSISTENT}[semantics], form, 0, 0)
     cand = None if candidates is None else np.ascontiguousarray(candidates, np.int32)
     n = 0 if cand is None else len(cand)
@@ -96,7 +97,7 @@ class FemContext:
         mesh, self._keep = _mesh_struct(p)
         mat = capi.Material(float(p.E), float(p.nu), float(p.rho))
         form = {"gradient": capi.FORM_GRADIENT, "stored_ke": capi.FORM_STORED_KE, "auto": capi.FORM_AUTO,
-                "fan": capi.FORM_GRADIENT_FAN}[matvec_form]
+                "fan": capi.FORM_GRADIENT_FAN, "geometry": capi.FORM_GEOMETRY_FAN}[matvec_form]
         opt = capi.Options({"compat": capi.COMPAT, "consistent": capi.CONSISTENT}[semantics], form, int(patch_elems),
                            int(verbose))
         h = C.c_void_p()

@@ -74,7 +74,9 @@ typedef enum cfem_matvec_form {
   CFEM_FORM_AUTO = 0,      /* edge fans in 3D, per element in 2D */
   CFEM_FORM_GRADIENT = 1,  /* stored scaled shape gradients: K_e p = G^T D G p, one thread per element */
   CFEM_FORM_STORED_KE = 2, /* stored 12x12 / 6x6 FP32 K_e (the reference's Klocals) */
-  CFEM_FORM_GRADIENT_FAN = 3 /* gradient form, one thread per edge fan of up to 6 tets (3D) */
+  CFEM_FORM_GRADIENT_FAN = 3, /* gradient form, one thread per edge fan of up to 6 tets (3D) */
+  CFEM_FORM_GEOMETRY_FAN = 4  /* edge fans; the FP32 matvec forms the gradients from streamed
+                                 patch-relative coordinates instead of reading stored ones (3D) */
 } cfem_matvec_form;
 
 typedef enum cfem_wavelet_type { CFEM_WAVELET_NONE = 0, CFEM_WAVELET_RICKER = 1, CFEM_WAVELET_BERLAGE = 2 } cfem_wavelet_type;
