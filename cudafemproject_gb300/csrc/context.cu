@@ -491,7 +491,7 @@ void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, co
         const int len = P.fan_slot[(size_t)(f0 + fl) * kFanSlots + kFanSlots - 1];
         for (int h = 0; h < 2; ++h)
           for (int hs = 0; hs < half_slot_count(h, len); ++hs)
-            ++cnt[P.fan_slot[(size_t)(f0 + fl) * kFanSlots + half_slot_to_fan(h, hs)] + 1];
+            if (half_writes(h, hs)) ++cnt[P.fan_slot[(size_t)(f0 + fl) * kFanSlots + half_slot_to_fan(h, hs)] + 1];
       }
       for (int i = 0; i < n; ++i) cnt[i + 1] += cnt[i];
       const int total = cnt[n];
@@ -500,8 +500,9 @@ void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, co
         const int len = P.fan_slot[(size_t)(f0 + fl) * kFanSlots + kFanSlots - 1];
         for (int h = 0; h < 2; ++h)
           for (int hs = 0; hs < half_slot_count(h, len); ++hs)
-            fp[(h * 6 + hs) * kFanThreads + fl] =
-                (uint16_t)cnt[P.fan_slot[(size_t)(f0 + fl) * kFanSlots + half_slot_to_fan(h, hs)]]++;
+            if (half_writes(h, hs))
+              fp[(h * 6 + hs) * kFanThreads + fl] =
+                  (uint16_t)cnt[P.fan_slot[(size_t)(f0 + fl) * kFanSlots + half_slot_to_fan(h, hs)]]++;
       }
       for (int i = 0; i < c->L32.npn; ++i) {
         nd[i] = i < n ? P.p_nodes[nb + i] : P.p_nodes[nb];

@@ -1,6 +1,7 @@
 // Edge-fan EbE matvec with the per-patch data streamed by bulk asynchronous
 // copies. Two threads share a fan: half h evaluates tets 3h .. 3h+2 and owns
-// the six node slots P, Q, R_3h .. R_3h+3 (kHalfSlots = 12 force slots per fan).
+// the six node slots P, Q, R_3h .. R_3h+3 (kHalfSlots = 12 slots per fan, of
+// which 9 distinct nodes: half 0 writes the shared P, Q, R_3 forces of both).
 // Everything a patch needs apart from the node vectors lives in one
 // contiguous, 128-byte aligned block of the "patch block" array:
 //   [header: 4 i32]                        patch nodes, first owned node, fans, 0
@@ -37,6 +38,27 @@ __host__ __device__ __forceinline__ int half_slot_to_fan(int h, int hs) { return
 // number of valid slots of half h of a fan of length len (0 if the half has no tet)
 __host__ __device__ __forceinline__ int half_slot_count(int h, int len) {
   return len > 3 * h ? 3 + (len - 3 * h < 3 ? len - 3 * h : 3) : 0;
+}
+// whether half h writes slot hs to the force list: the halves share P, Q and
+// R_3 (slot 5 of half 0 = slot 2 of half 1), whose forces half 0 writes after
+// a lane shuffle with half 1 (combine_half_forces)
+__host__ __device__ __forceinline__ bool half_writes(int h, int hs) { return h == 0 || hs >= 3; }
+
+// Adds half 1's P, Q and R_3 forces to half 0's (lanes 2f and 2f + 1); every
+// lane of the warp takes part.
+template <typename T, int DIM>
+__device__ __forceinline__ void combine_half_forces(T (&fv)[6][DIM], int h) {
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    const T p = __shfl_xor_sync(0xffffffffu, fv[0][d], 1);
+    const T q = __shfl_xor_sync(0xffffffffu, fv[1][d], 1);
+    const T r = __shfl_xor_sync(0xffffffffu, h ? fv[2][d] : fv[5][d], 1);
+    if (h == 0) {
+      fv[0][d] += p;
+      fv[1][d] += q;
+      fv[5][d] += r;
+    }
+  }
 }
 
 struct FanBlockLayout {
@@ -77,7 +99,7 @@ inline FanBlockLayout fan_geo_block_layout(int np_max, bool with_scale) {
   return L;
 }
 
-constexpr int kForceBytes = kHalfSlots * kFanThreads * 16;  // separate force list of geometry blocks
+constexpr int kForceBytes = 9 * kFanThreads * 16;  // separate force list of geometry blocks (9 entries per fan)
 
 // Geometry blocks: two buffers, the force list, and two stages of the node
 // vectors a PCG-form matvec reads (z and p_old), gathered one patch ahead.
@@ -384,9 +406,10 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
     // read its gradients, or (GEO) the separate force region
     if (!GEO) __syncthreads();
     T *fs = GEO ? fgeo : reinterpret_cast<T *>(B + L.g_off);
+    combine_half_forces<T, DIM>(fv, h);
 #pragma unroll
     for (int k = 0; k < 6; ++k)
-      if (k < nk) {
+      if (k < nk && half_writes(h, k)) {
         NodeV<T, VW> o;
 #pragma unroll
         for (int d = 0; d < VW; ++d) o.v[d] = d < DIM ? fv[k][d] : T(0);
@@ -405,6 +428,7 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
       const unsigned bb = bits[i];
       T acc3[DIM] = {0, 0, 0};
       const int k1 = fstart[i + 1];
+#pragma unroll 4
       for (int k = fstart[i]; k < k1; ++k) {
         const NodeV<T, VW> fo = ldv<T, VW>(fs, k);
 #pragma unroll

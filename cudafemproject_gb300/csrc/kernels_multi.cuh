@@ -185,10 +185,12 @@ __global__ void __launch_bounds__(kHfanThreads) k_matvec_multi(MultiParams<float
         }
       }
 #pragma unroll
+      for (int r = 0; r < R; ++r) combine_half_forces<T, DIM>(fv[r], h);
+#pragma unroll
       for (int r = 0; r < R; ++r)
 #pragma unroll
         for (int k = 0; k < 6; ++k)
-          if (k < nk) {
+          if (k < nk && half_writes(h, k)) {
             NodeV<T, VW> o;
 #pragma unroll
             for (int d = 0; d < VW; ++d) o.v[d] = d < DIM ? fv[r][k][d] : T(0);
