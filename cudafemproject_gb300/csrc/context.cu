@@ -471,8 +471,8 @@ void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, co
     std::vector<unsigned char> hb(pre * P.n_patches, 0);
     for (int p = 0; p < P.n_patches; ++p) {
       unsigned char *B = hb.data() + pre * p;
-      uint16_t *sl = reinterpret_cast<uint16_t *>(B + c->L32.slot_off);
-      uint16_t *fp = reinterpret_cast<uint16_t *>(B + c->L32.fpos_off);
+      uint32_t *sl = reinterpret_cast<uint32_t *>(B + c->L32.slot_off);
+      uint32_t *fp = reinterpret_cast<uint32_t *>(B + c->L32.fpos_off);
       uint16_t *fst = reinterpret_cast<uint16_t *>(B + c->L32.fstart_off);
       int32_t *nd = reinterpret_cast<int32_t *>(B + c->L32.nodes_off);
       uint8_t *bt = B + c->L32.bits_off;
@@ -483,8 +483,17 @@ void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, co
       hdr[1] = P.p_own[p];
       hdr[2] = nf;
       hdr[3] = 0;
-      for (int fl = 0; fl < nf; ++fl)
-        for (int k = 0; k < kFanSlots; ++k) sl[k * kFanThreads + fl] = P.fan_slot[(size_t)(f0 + fl) * kFanSlots + k];
+      // slots of half-thread t = 2 fl + h (kNoSlot where absent), two per word
+      for (int t = 0; t < kHfanThreads; ++t) {
+        const int fl = t >> 1, h = t & 1;
+        const int len = fl < nf ? P.fan_slot[(size_t)(f0 + fl) * kFanSlots + kFanSlots - 1] : 0;
+        for (int k = 0; k < 6; ++k) {
+          const uint32_t v = k < half_slot_count(h, len)
+                                 ? P.fan_slot[(size_t)(f0 + fl) * kFanSlots + half_slot_to_fan(h, k)]
+                                 : kNoSlot;
+          sl[(k >> 1) * kHfanThreads + t] |= v << (16 * (k & 1));
+        }
+      }
       // half-fan incidences (fan fl, half h, slot hs), counting-sorted by node
       std::vector<int> cnt(n + 1, 0);
       for (int fl = 0; fl < nf; ++fl) {
@@ -500,9 +509,10 @@ void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, co
         const int len = P.fan_slot[(size_t)(f0 + fl) * kFanSlots + kFanSlots - 1];
         for (int h = 0; h < 2; ++h)
           for (int hs = 0; hs < half_slot_count(h, len); ++hs)
-            if (half_writes(h, hs))
-              fp[(h * 6 + hs) * kFanThreads + fl] =
-                  (uint16_t)cnt[P.fan_slot[(size_t)(f0 + fl) * kFanSlots + half_slot_to_fan(h, hs)]]++;
+            if (half_writes(h, hs)) {
+              const uint32_t pos = (uint32_t)cnt[P.fan_slot[(size_t)(f0 + fl) * kFanSlots + half_slot_to_fan(h, hs)]]++;
+              fp[(hs >> 1) * kHfanThreads + 2 * fl + h] |= pos << (16 * (hs & 1));
+            }
       }
       for (int i = 0; i < c->L32.npn; ++i) {
         nd[i] = i < n ? P.p_nodes[nb + i] : P.p_nodes[nb];

@@ -5,11 +5,16 @@
 // Everything a patch needs apart from the node vectors lives in one
 // contiguous, 128-byte aligned block of the "patch block" array:
 //   [header: 4 i32]                        patch nodes, first owned node, fans, 0
-//   [slot: kFanSlots x kFanThreads u16]   patch-local nodes P, Q, R_0.. of each fan, then its length
-//   [fpos: kHalfSlots x kFanThreads u16]  position of each (fan, half slot) force in the node-sorted list
+//   [slot: 3 x kHfanThreads u32]           patch-local nodes of the six slots of half-thread t = 2 fan + h,
+//                                          two u16 per word (slot 2q low, 2q+1 high), kNoSlot if absent
+//   [fpos: 3 x kHfanThreads u32]           position of each written slot force in the node-sorted list
 //   [fstart: nps u16]                      node i sums forces fstart[i] .. fstart[i+1]-1
 //   [nodes: npn i32] [bits: npn u8]        global node ids and constraint bits of the patch nodes
-//   [G: 9 kFanMax x kFanThreads T]         scaled gradients in fan vertex order, row (j*9 + (b-1)*3 + d)
+//   [G: 3 x (2 x kHfanThreads float4 + kHfanThreads float)]
+//                                          scaled gradients of tet jj of half-thread t in fan vertex
+//                                          order (row (b-1)*3 + d): rows 0-3, rows 4-7, row 8
+// The per-half-thread tables are thread-interleaved, so the two halves of a
+// fan (adjacent lanes) never read the same bank.
 // One copy per patch, issued two patches ahead into a double buffer, so the
 // operator stream overlaps the arithmetic of the current patch. The forces of
 // a patch are written into the G region of its own buffer once every thread
@@ -32,6 +37,7 @@ namespace cfem {
 constexpr int kStageUnroll = 2;      // node gathers in flight per thread while staging a patch
 constexpr int kHalfSlots = 12;       // force slots per fan: 2 halves x (P, Q, 4 ring vertices)
 constexpr int kHfanThreads = 2 * kFanThreads;
+constexpr uint16_t kNoSlot = 0xFFFF;  // absent slot of a half-thread
 
 // fan slot (0 = P, 1 = Q, 2 + k = R_k) of half h's slot hs
 __host__ __device__ __forceinline__ int half_slot_to_fan(int h, int hs) { return hs < 2 ? hs : hs + 3 * h; }
@@ -61,6 +67,43 @@ __device__ __forceinline__ void combine_half_forces(T (&fv)[6][DIM], int h) {
   }
 }
 
+// Slots of half-thread t: patch-local node indices, and how many are valid
+// (a prefix: 3 + the half's tets, or 0).
+__device__ __forceinline__ int load_half_slots(const unsigned char *slot_tab, int t, int (&s)[6]) {
+  const uint32_t *w = reinterpret_cast<const uint32_t *>(slot_tab);
+  int nk = 0;
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    const uint32_t v = w[q * kHfanThreads + t];
+    s[2 * q] = (int)(v & 0xFFFFu);
+    s[2 * q + 1] = (int)(v >> 16);
+  }
+#pragma unroll
+  for (int k = 0; k < 6; ++k) nk += s[k] != kNoSlot;
+  return nk;
+}
+
+// Force-list position of slot k of half-thread t.
+__device__ __forceinline__ int half_fpos(const unsigned char *fpos_tab, int t, int k) {
+  const uint32_t v = reinterpret_cast<const uint32_t *>(fpos_tab)[(k >> 1) * kHfanThreads + t];
+  return (int)((k & 1) ? v >> 16 : v & 0xFFFFu);
+}
+
+// Scaled gradients of tet jj of half-thread t (2 float4 + 1 float).
+__device__ __forceinline__ void load_tet_G(const unsigned char *g_tab, int t, int jj, float (&G)[9]) {
+  const unsigned char *base = g_tab + (size_t)jj * (9 * kHfanThreads * 4);
+  const float4 a = reinterpret_cast<const float4 *>(base)[t];
+  const float4 b = reinterpret_cast<const float4 *>(base)[kHfanThreads + t];
+  G[0] = a.x; G[1] = a.y; G[2] = a.z; G[3] = a.w;
+  G[4] = b.x; G[5] = b.y; G[6] = b.z; G[7] = b.w;
+  G[8] = reinterpret_cast<const float *>(base + 2 * kHfanThreads * 16)[t];
+}
+// byte offset of gradient row k of tet jj of half-thread t inside the G region
+__host__ __device__ __forceinline__ int tet_G_offset(int t, int jj, int k) {
+  const int base = jj * (9 * kHfanThreads * 4);
+  return k < 8 ? base + ((k >> 2) * kHfanThreads + t) * 16 + (k & 3) * 4 : base + 2 * kHfanThreads * 16 + t * 4;
+}
+
 struct FanBlockLayout {
   int bytes;        // per patch, multiple of 128
   int hdr_off, slot_off, fpos_off, fstart_off, nodes_off, bits_off;
@@ -76,8 +119,8 @@ inline FanBlockLayout fan_block_layout(int np_max, size_t tsize) {
   L.npn = up(np_max, 4);
   int off = 0;
   L.hdr_off = off; off += 16;
-  L.slot_off = off; off += kFanSlots * kFanThreads * 2;
-  L.fpos_off = off; off += kHalfSlots * kFanThreads * 2;
+  L.slot_off = off; off += 3 * kHfanThreads * 4;
+  L.fpos_off = off; off += 3 * kHfanThreads * 4;
   L.fstart_off = off; off += L.nps * 2;
   L.nodes_off = off; off += L.npn * 4;
   L.bits_off = off; off += up(L.npn, 16);
@@ -147,7 +190,7 @@ struct FanTmaParams {
 template <typename T, int MODE, bool GEO = false>
 // (3 CTAs per SM: the shared memory of a CTA allows 3, the register bound makes them fit)
 __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> P, FanTmaParams F) {
-  static_assert(!GEO || sizeof(T) == 4, "geometry blocks are FP32");
+  static_assert(sizeof(T) == 4, "patch blocks are FP32");
   constexpr int DIM = 3, VW = 4;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const FanBlockLayout &L = F.L;
@@ -211,13 +254,11 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
       }
       return;
     }
-    const uint16_t *sl = reinterpret_cast<const uint16_t *>(B + L.slot_off);
-    const uint16_t *fpos = reinterpret_cast<const uint16_t *>(B + L.fpos_off);
     const uint16_t *fstart = reinterpret_cast<const uint16_t *>(B + L.fstart_off);
     const int32_t *nodes = reinterpret_cast<const int32_t *>(B + L.nodes_off);
     const uint8_t *bits = B + L.bits_off;
     const int32_t *hdr = reinterpret_cast<const int32_t *>(B + L.hdr_off);
-    const int nn = hdr[0], own = hdr[1], nf = hdr[2];
+    const int nn = hdr[0], own = hdr[1];
     bool skip = false;
     if (batch) {  // the patch's instance: material, direction update, convergence mask
       lam = P.pmat[2 * patch];
@@ -295,8 +336,8 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
     //    Missing tets have zero gradients, so the three tets are straight-line
     //    code; differences to P are formed once per node slot.
     const int fl = threadIdx.x >> 1, h = threadIdx.x & 1;
-    const int len = fl < nf ? sl[(kFanSlots - 1) * kFanThreads + fl] : 0;
-    const int nk = half_slot_count(h, len);
+    int slot[6];
+    const int nk = load_half_slots(B + L.slot_off, threadIdx.x, slot);
     T fv[6][DIM];
     {
       T du[6][DIM];  // node values of the slots (differences to P after step a)
@@ -308,9 +349,8 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
 #pragma unroll
         for (int d = 0; d < VW; ++d) s.v[d] = xk.v[d] = 0;
         if (k < nk) {
-          const int slot = sl[half_slot_to_fan(h, k) * kFanThreads + fl];
-          s = ldv<T, VW>(spp, slot);
-          if (GEO) xk = ldv<T, VW>(reinterpret_cast<const T *>(Xs), slot);
+          s = ldv<T, VW>(spp, slot[k]);
+          if (GEO) xk = ldv<T, VW>(reinterpret_cast<const T *>(Xs), slot[k]);
         }
 #pragma unroll
         for (int d = 0; d < DIM; ++d) {
@@ -330,11 +370,9 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
         const int j = 3 * h + jj;
         if constexpr (GEO) {
           const float sc = L.c_off >= 0 ? reinterpret_cast<const float *>(B + L.c_off)[j * kFanThreads + fl] : 1.0f;
-          geo_gradients(dx[1], dx[2 + jj], dx[3 + jj], sc, j < len, G);
+          geo_gradients(dx[1], dx[2 + jj], dx[3 + jj], sc, jj + 3 < nk, G);
         } else {
-          const T *Gs = reinterpret_cast<const T *>(B + L.g_off);
-#pragma unroll
-          for (int k = 0; k < 9; ++k) G[k] = Gs[(j * 9 + k) * kFanThreads + fl];
+          load_tet_G(B + L.g_off, threadIdx.x, jj, G);
         }
       };
       if (P.mcoef == nullptr) {
@@ -371,7 +409,7 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
 #pragma unroll
         for (int jj = 0; jj < 3; ++jj) {
           const int j = 3 * h + jj;
-          if (nk && j < len) {
+          if (jj + 3 < nk) {
             T G[9];
             tet_G(jj, G);
             T u[4][DIM], fe[4][DIM];
@@ -413,7 +451,7 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
         NodeV<T, VW> o;
 #pragma unroll
         for (int d = 0; d < VW; ++d) o.v[d] = d < DIM ? fv[k][d] : T(0);
-        stv<T, VW>(fs, fpos[(h * 6 + k) * kFanThreads + fl], o);
+        stv<T, VW>(fs, half_fpos(B + L.fpos_off, threadIdx.x, k), o);
       }
     if constexpr (PREFETCH) {  // the next patch's gathers overlap the node sums below
       if (patch + step < P.n_patches &&
@@ -564,16 +602,15 @@ static __global__ void k_fan_block_gradients(int64_t ne, const double *G64, int6
   const int f = fp >> 3, j = fp & 7;
   const int p = fan_patch[f];
   const int fl = f - fan_off[p];
-  float *G32b = reinterpret_cast<float *>(blk32 + (size_t)p * L32.bytes + L32.g_off);
+  const int t = 2 * fl + j / 3, jj = j % 3;  // half-thread and its tet
+  unsigned char *G32b = blk32 + (size_t)p * L32.bytes + L32.g_off;
   const unsigned perm = fan_perm[e];
 #pragma unroll
   for (int b = 1; b < 4; ++b) {
     const int a = (perm >> (2 * b)) & 3u;
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      const int row = j * 9 + (b - 1) * 3 + d;
-      G32b[row * kFanThreads + fl] = (float)g[a][d];
-    }
+    for (int d = 0; d < 3; ++d)
+      *reinterpret_cast<float *>(G32b + tet_G_offset(t, jj, (b - 1) * 3 + d)) = (float)g[a][d];
   }
 }
 

@@ -74,12 +74,9 @@ __global__ void __launch_bounds__(kHfanThreads) k_matvec_multi(MultiParams<float
     fence_mbar_init();
   }
   __syncthreads();
-  const uint16_t *sl = reinterpret_cast<const uint16_t *>(B + L.slot_off);
-  const uint16_t *fpos = reinterpret_cast<const uint16_t *>(B + L.fpos_off);
   const uint16_t *fstart = reinterpret_cast<const uint16_t *>(B + L.fstart_off);
   const int32_t *nodes = reinterpret_cast<const int32_t *>(B + L.nodes_off);
   const uint8_t *bits = B + L.bits_off;
-  const T *Gs = reinterpret_cast<const T *>(B + L.g_off);
   int it = 0;
   for (int patch = blockIdx.x; patch < P.n_patches; patch += gridDim.x, ++it) {
     fence_proxy_async();  // earlier reads of the block precede the copy that overwrites it
@@ -94,10 +91,10 @@ __global__ void __launch_bounds__(kHfanThreads) k_matvec_multi(MultiParams<float
       return;
     }
     const int32_t *hdr = reinterpret_cast<const int32_t *>(B + L.hdr_off);
-    const int nn = hdr[0], own = hdr[1], nf = hdr[2];
-    const int fl = threadIdx.x >> 1, h = threadIdx.x & 1;
-    const int len = fl < nf ? sl[(kFanSlots - 1) * kFanThreads + fl] : 0;
-    const int nk = half_slot_count(h, len);
+    const int nn = hdr[0], own = hdr[1];
+    const int h = threadIdx.x & 1;
+    int slot[6];
+    const int nk = load_half_slots(B + L.slot_off, threadIdx.x, slot);
     for (int c0 = 0; c0 < K; c0 += R) {
       if (MODE == MV_PCG) {
         // every thread evaluates the pass's cases itself; the barrier's AND
@@ -137,7 +134,7 @@ __global__ void __launch_bounds__(kHfanThreads) k_matvec_multi(MultiParams<float
         T uv[R][6][DIM];
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
-          const int li = k < nk ? sl[half_slot_to_fan(h, k) * kFanThreads + fl] : 0;
+          const int li = k < nk ? slot[k] : 0;
 #pragma unroll
           for (int r = 0; r < R; ++r) {
             NodeV<T, VW> s;
@@ -155,11 +152,9 @@ __global__ void __launch_bounds__(kHfanThreads) k_matvec_multi(MultiParams<float
         for (int r = 0; r < R; ++r) e_fan[r] = 0;
 #pragma unroll
         for (int jj = 0; jj < 3; ++jj) {
-          const int j = 3 * h + jj;
-          if (nk && j < len) {
+          if (jj + 3 < nk) {
             T G[9];
-#pragma unroll
-            for (int k = 0; k < 9; ++k) G[k] = Gs[(j * 9 + k) * kFanThreads + fl];
+            load_tet_G(B + L.g_off, threadIdx.x, jj, G);
 #pragma unroll
             for (int r = 0; r < R; ++r) {
               T u[4][DIM], fe[4][DIM];
@@ -194,7 +189,7 @@ __global__ void __launch_bounds__(kHfanThreads) k_matvec_multi(MultiParams<float
             NodeV<T, VW> o;
 #pragma unroll
             for (int d = 0; d < VW; ++d) o.v[d] = d < DIM ? fv[r][k][d] : T(0);
-            stv<T, VW>(fs, (int64_t)fpos[(h * 6 + k) * kFanThreads + fl] * R + r, o);
+            stv<T, VW>(fs, (int64_t)half_fpos(B + L.fpos_off, threadIdx.x, k) * R + r, o);
           }
       __syncthreads();
       // 3. node sums: items (node i, case r)
