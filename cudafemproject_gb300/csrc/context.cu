@@ -54,9 +54,12 @@ void launch_mv_t(cfem_ctx *c, int mode, const MvParams<T> &P) {
       F.fan_off = c->fan_off.p;
       F.fan_elem_off = c->fan_elem_off.p;
       F.err = c->tma_err.p;
+      const double l2_half = 0.5 * c->l2_bytes;
+      F.evict_first = (double)c->L32.bytes * c->prep.n_patches > l2_half;
       if (c->geo && !P.patch_inst) {
         F.blocks = c->blkg.p;
         F.L = c->Lg;
+        F.evict_first = (double)c->Lg.bytes * c->prep.n_patches > l2_half;
         dim3 g(c->grid_geo), b(kHfanThreads);
         if (mode == MV_PLAIN) k_matvec_fan_tma<float, MV_PLAIN, true><<<g, b, c->smem_geo, c->stream>>>(P, F);
         else if (mode == MV_PCG) k_matvec_fan_tma<float, MV_PCG, true><<<g, b, c->smem_geo, c->stream>>>(P, F);
@@ -416,6 +419,7 @@ void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, co
   }
   CK(cudaGetDevice(&c->device));
   CK(cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, c->device));
+  CK(cudaDeviceGetAttribute(&c->l2_bytes, cudaDevAttrL2CacheSize, c->device));
   int pe = opt && opt->patch_elems > 0 ? opt->patch_elems : (c->fans ? kFanMax * kFanThreads : 512);
   // the per-incidence force slots of a patch must fit in shared memory
   pe = std::min(std::max((pe + 31) / 32 * 32, 32), m->dim == 2 ? 2048 : 1024);

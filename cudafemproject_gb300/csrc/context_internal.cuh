@@ -100,7 +100,7 @@ struct cfem_ctx {
   cudaStream_t user_stream = nullptr;  // the caller's stream; work is ordered after it
   bool own_stream = false;
   cudaEvent_t ev_in = nullptr;
-  int device = 0, n_sm = 0;
+  int device = 0, n_sm = 0, l2_bytes = 0;
   int dim = 0, nv = 0, w = 0, vw = 0, ncomp = 0;
   int64_t nn = 0, ne = 0, nd = 0, nvec = 0;
   int semantics = 0, form = CFEM_FORM_GRADIENT, verbose = 0;

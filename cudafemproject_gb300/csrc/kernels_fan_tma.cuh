@@ -185,6 +185,8 @@ struct FanTmaParams {
   const int32_t *fan_off;       // [n_patches + 1]
   const int32_t *fan_elem_off;  // [n_fans + 1] (consistent-mass coefficients)
   int *err;                     // kErrTmaTimeout on a copy that never completed
+  int evict_first;              // blocks larger than about half the L2: stream them with an
+                                // evict-first policy, so that the node vectors stay resident
 };
 
 template <typename T, int MODE, bool GEO = false>
@@ -210,10 +212,12 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
   T beta = 0;
   if (MODE == MV_PCG && !batch) beta = T(P.sc->beta);
   T lam = P.lam, mu = P.mu;
+  __shared__ unsigned warps_done[2];  // warps finished with buffer 0 / 1 (see the end of the patch loop)
   if (threadIdx.x == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
     fence_mbar_init();
+    warps_done[0] = warps_done[1] = 0;
   }
   __syncthreads();
   const int step = gridDim.x;
@@ -222,7 +226,11 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
       const int q = blockIdx.x + k * step;
       if (q < P.n_patches) {
         mbar_expect_tx(&bar[k], (unsigned)L.bytes);
-        bulk_load(k ? buf1 : buf0, F.blocks + (size_t)q * L.bytes, (unsigned)L.bytes, &bar[k]);
+        if (F.evict_first)
+          bulk_load_hint(k ? buf1 : buf0, F.blocks + (size_t)q * L.bytes, (unsigned)L.bytes, &bar[k],
+                         l2_evict_first_policy());
+        else
+          bulk_load(k ? buf1 : buf0, F.blocks + (size_t)q * L.bytes, (unsigned)L.bytes, &bar[k]);
       }
     }
   }
@@ -245,20 +253,26 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
   for (int patch = blockIdx.x; patch < P.n_patches; patch += step, ++it) {
     const int b = it & 1;
     unsigned char *B = b ? buf1 : buf0;
+    // Every thread waits for the block itself; the staging barrier below
+    // makes a failed copy a uniform exit (a thread whose wait failed reads
+    // nothing of the block before it).
     const bool ok = mbar_wait_bounded(&bar[b], (unsigned)((it >> 1) & 1));
-    if (__syncthreads_or(!ok)) {
+    auto copy_failed = [&]() {
       if (PREFETCH) cp_async_wait<0>();
       if (threadIdx.x == 0) {
         atomicOr(F.err, kErrTmaTimeout);
         if (patch + step < P.n_patches) mbar_wait_bounded(&bar[b ^ 1], (unsigned)(((it + 1) >> 1) & 1));
       }
+    };
+    if (batch && __syncthreads_or(!ok)) {  // (uniform: batch is a kernel parameter)
+      copy_failed();
       return;
     }
     const uint16_t *fstart = reinterpret_cast<const uint16_t *>(B + L.fstart_off);
     const int32_t *nodes = reinterpret_cast<const int32_t *>(B + L.nodes_off);
     const uint8_t *bits = B + L.bits_off;
     const int32_t *hdr = reinterpret_cast<const int32_t *>(B + L.hdr_off);
-    const int nn = hdr[0], own = hdr[1];
+    const int nn = ok ? hdr[0] : 0, own = ok ? hdr[1] : 0;
     bool skip = false;
     if (batch) {  // the patch's instance: material, direction update, convergence mask
       lam = P.pmat[2 * patch];
@@ -275,7 +289,10 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
       // 1. the gathered z and p_old of this patch: p = z + beta p_old, owned
       //    nodes written out, constrained DOFs masked, in place
       cp_async_wait<0>();
-      __syncthreads();
+      if (__syncthreads_or(!ok)) {
+        copy_failed();
+        return;
+      }
       spp = sp + (size_t)(it & 1) * stage_stride;
       for (int i = threadIdx.x; i < nn; i += kHfanThreads) {
         NodeV<T, VW> v = ldv<T, VW>(spp, i);
@@ -331,7 +348,10 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
       }
     }
     }  // PREFETCH
-    __syncthreads();
+    if (__syncthreads_or(!ok)) {
+      copy_failed();
+      return;
+    }
     // 2. half a fan per thread (tets 3h .. 3h+2), forces kept in registers.
     //    Missing tets have zero gradients, so the three tets are straight-line
     //    code; differences to P are formed once per node slot.
@@ -510,14 +530,26 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
       if (threadIdx.x == 0) P.patch_energy[patch] = t;
       energy = DotAcc<T>();
     }
-    // Buffer b is free again. Every thread orders its own generic-proxy
-    // accesses of it (the force stores and reads) before the bulk copy that
-    // refills it, then the barrier makes that true for all of them.
+    // Buffer b is free again once every warp is done with it. Each thread
+    // orders its own generic-proxy accesses of the buffer before the bulk copy
+    // that refills it; the last warp to finish issues that copy, so the other
+    // warps go on to the next patch without waiting here.
     fence_proxy_async();
-    __syncthreads();
-    if (threadIdx.x == 0 && patch + 2 * step < P.n_patches) {
-      mbar_expect_tx(&bar[b], (unsigned)L.bytes);
-      bulk_load(B, F.blocks + (size_t)(patch + 2 * step) * L.bytes, (unsigned)L.bytes, &bar[b]);
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0) {
+      __threadfence_block();
+      if (atomicAdd(&warps_done[b], 1u) == kHfanThreads / 32 - 1) {
+        __threadfence_block();
+        warps_done[b] = 0;
+        if (patch + 2 * step < P.n_patches) {
+          mbar_expect_tx(&bar[b], (unsigned)L.bytes);
+          const unsigned char *src = F.blocks + (size_t)(patch + 2 * step) * L.bytes;
+          if (F.evict_first)
+            bulk_load_hint(B, src, (unsigned)L.bytes, &bar[b], l2_evict_first_policy());
+          else
+            bulk_load(B, src, (unsigned)L.bytes, &bar[b]);
+        }
+      }
     }
   }
   if (MODE == MV_PCG && !batch) {
