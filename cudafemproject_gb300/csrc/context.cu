@@ -39,6 +39,24 @@ MvParams<T> base_mv_t(cfem_ctx *c) {
   return P;
 }
 
+// Launch with programmatic stream serialization: the kernel may start while
+// the previous kernel in the stream runs (it calls griddep_wait before reading
+// that kernel's results). Used for the matvec / update pairs of the PCG loop.
+template <typename... KArgs, typename... Args>
+static void launch_pdl(void (*kern)(KArgs...), dim3 g, dim3 b, size_t smem, cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = g;
+  cfg.blockDim = b;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  CK(cudaLaunchKernelEx(&cfg, kern, args...));
+}
+
 template <typename T>
 void launch_mv_t(cfem_ctx *c, int mode, const MvParams<T> &P) {
   if (c->n_inst && !P.patch_inst)
@@ -62,7 +80,7 @@ void launch_mv_t(cfem_ctx *c, int mode, const MvParams<T> &P) {
         F.evict_first = (double)c->Lg.bytes * c->prep.n_patches > l2_half;
         dim3 g(c->grid_geo), b(kHfanThreads);
         if (mode == MV_PLAIN) k_matvec_fan_tma<float, MV_PLAIN, true><<<g, b, c->smem_geo, c->stream>>>(P, F);
-        else if (mode == MV_PCG) k_matvec_fan_tma<float, MV_PCG, true><<<g, b, c->smem_geo, c->stream>>>(P, F);
+        else if (mode == MV_PCG) launch_pdl(k_matvec_fan_tma<float, MV_PCG, true>, g, b, c->smem_geo, c->stream, P, F);
         else k_matvec_fan_tma<float, MV_DYN, true><<<g, b, c->smem_geo, c->stream>>>(P, F);
         CKL();
         c->launches += 1;
@@ -70,7 +88,7 @@ void launch_mv_t(cfem_ctx *c, int mode, const MvParams<T> &P) {
       }
       dim3 g(c->grid_ft32), b(kHfanThreads);
       if (mode == MV_PLAIN) k_matvec_fan_tma<float, MV_PLAIN><<<g, b, c->smem_ft32, c->stream>>>(P, F);
-      else if (mode == MV_PCG) k_matvec_fan_tma<float, MV_PCG><<<g, b, c->smem_ft32, c->stream>>>(P, F);
+      else if (mode == MV_PCG) launch_pdl(k_matvec_fan_tma<float, MV_PCG>, g, b, c->smem_ft32, c->stream, P, F);
       else k_matvec_fan_tma<float, MV_DYN><<<g, b, c->smem_ft32, c->stream>>>(P, F);
       CKL();
       c->launches += 1;
@@ -127,7 +145,7 @@ void launch_init(cfem_ctx *c, const VecParams<T> &P, int warm) {
 
 template <typename T>
 void launch_update(cfem_ctx *c, const VecParams<T> &P) {
-  if (c->dim == 3) k_pcg_update<T, 3><<<c->grid_vec, kThreads, 0, c->stream>>>(P);
+  if (c->dim == 3) launch_pdl(k_pcg_update<T, 3>, dim3(c->grid_upd), dim3(kThreads), 0, c->stream, P);
   else k_pcg_update<T, 2><<<c->grid_vec, kThreads, 0, c->stream>>>(P);
   CKL();
   c->launches += 1;
@@ -674,6 +692,9 @@ void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, co
     }
   }
   c->grid_vec = (int)std::min<int64_t>(std::max<int64_t>(1, nblk(c->nn)), (int64_t)c->n_sm * 4);
+  // PCG update: two CTAs per SM keep enough loads in flight for the bandwidth
+  // and leave room for the next matvec's CTAs to start early (PDL)
+  c->grid_upd = (int)std::min<int64_t>(std::max<int64_t>(1, nblk(c->nn)), (int64_t)c->n_sm * 2);
   if (c->geo) {  // the grid of the largest geometry layout fits every later one
     int og = 1;
     const size_t smem_max = fan_tma_smem_bytes(fan_geo_block_layout(P.np_max, true), sizeof(float));

@@ -101,6 +101,7 @@ struct cfem_ctx {
   bool own_stream = false;
   cudaEvent_t ev_in = nullptr;
   int device = 0, n_sm = 0, l2_bytes = 0;
+  int grid_upd = 0;  // PCG update kernel (3D)
   int dim = 0, nv = 0, w = 0, vw = 0, ncomp = 0;
   int64_t nn = 0, ne = 0, nd = 0, nvec = 0;
   int semantics = 0, form = CFEM_FORM_GRADIENT, verbose = 0;

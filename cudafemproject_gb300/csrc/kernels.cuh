@@ -28,6 +28,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "tma.cuh"
+
 namespace cfem {
 
 constexpr int kThreads = 256;
@@ -621,33 +623,54 @@ __global__ void __launch_bounds__(kThreads) k_pcg_init(VecParams<T> P, int warm)
 
 // alpha = gamma / p.Ap; x += alpha p; r -= alpha u; u = 0; z = M^-1 r; gamma' = r.z
 template <typename T, int DIM>
-__global__ void __launch_bounds__(kThreads) k_pcg_update(VecParams<T> P) {
+__global__ void __launch_bounds__(kThreads, 2) k_pcg_update(VecParams<T> P) {
   constexpr int VW = DIM == 3 ? 4 : 2;
+  griddep_wait();               // alpha and A p come from the matvec before it
+  griddep_launch_dependents();  // the next matvec may start streaming its blocks
   Scalars *s = P.sc;
   if (s->done) return;
   const double alpha_d = s->alpha;
   const T alpha = (T)alpha_d;
   DotAcc<T> acc[2];
-  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < P.n_nodes; n += (int64_t)gridDim.x * blockDim.x) {
-    NodeV<T, VW> x = ldv<T, VW>(P.x, n), r = ldv<T, VW>(P.r, n), p = ldv<T, VW>(P.p, n), u = ldv<T, VW>(P.u, n);
-    NodeV<T, VW> di = ldv<T, VW>(P.dinv, n), z, zero;
+  // U nodes per thread per round, all their loads issued before any is used
+  constexpr int U = sizeof(T) == 4 ? 4 : 2;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x * U;
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x * U + threadIdx.x; base < P.n_nodes; base += stride) {
+    NodeV<T, VW> x[U], r[U], p[U], u[U], di[U];
 #pragma unroll
-    for (int d = 0; d < VW; ++d) { zero.v[d] = 0; z.v[d] = 0; }
-    T rz = 0, rr = 0;
-#pragma unroll
-    for (int d = 0; d < DIM; ++d) {
-      x.v[d] += alpha * p.v[d];
-      r.v[d] -= alpha * u.v[d];
-      z.v[d] = r.v[d] * di.v[d];
-      rz += r.v[d] * z.v[d];
-      rr += r.v[d] * r.v[d];
+    for (int q = 0; q < U; ++q) {
+      const int64_t n = base + (int64_t)q * blockDim.x;
+      if (n < P.n_nodes) {
+        x[q] = ldv<T, VW>(P.x, n);
+        r[q] = ldv<T, VW>(P.r, n);
+        p[q] = ldv<T, VW>(P.p, n);
+        u[q] = ldv<T, VW>(P.u, n);
+        di[q] = ldv<T, VW>(P.dinv, n);
+      }
     }
-    acc[0].add(rz);
-    acc[1].add(rr);
-    stv<T, VW>(P.x, n, x);
-    stv<T, VW>(P.r, n, r);
-    stv<T, VW>(P.z, n, z);
-    stv<T, VW>(P.u, n, zero);
+#pragma unroll
+    for (int q = 0; q < U; ++q) {
+      const int64_t n = base + (int64_t)q * blockDim.x;
+      if (n >= P.n_nodes) continue;
+      NodeV<T, VW> z, zero;
+#pragma unroll
+      for (int d = 0; d < VW; ++d) { zero.v[d] = 0; z.v[d] = 0; }
+      T rz = 0, rr = 0;
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) {
+        x[q].v[d] += alpha * p[q].v[d];
+        r[q].v[d] -= alpha * u[q].v[d];
+        z.v[d] = r[q].v[d] * di[q].v[d];
+        rz += r[q].v[d] * z.v[d];
+        rr += r[q].v[d] * r[q].v[d];
+      }
+      acc[0].add(rz);
+      acc[1].add(rr);
+      stv<T, VW>(P.x, n, x[q]);
+      stv<T, VW>(P.r, n, r[q]);
+      stv<T, VW>(P.z, n, z);
+      stv<T, VW>(P.u, n, zero);
+    }
   }
   double tot[2];
   if (grid_sum_acc<2, T>(acc, tot, P.partials, &s->count_up)) {

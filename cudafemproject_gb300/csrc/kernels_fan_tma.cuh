@@ -208,9 +208,6 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
   constexpr bool PREFETCH = GEO && MODE == MV_PCG;
   const int stage_stride = 2 * L.npn * VW;
   const bool batch = P.patch_inst != nullptr;
-  if (MODE == MV_PCG && (batch ? P.bctl->all_done : P.sc->done)) return;
-  T beta = 0;
-  if (MODE == MV_PCG && !batch) beta = T(P.sc->beta);
   T lam = P.lam, mu = P.mu;
   __shared__ unsigned warps_done[2];  // warps finished with buffer 0 / 1 (see the end of the patch loop)
   if (threadIdx.x == 0) {
@@ -234,6 +231,17 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
       }
     }
   }
+  // The first two blocks (static operator data) are on their way; everything
+  // below reads what the previous kernel in the stream wrote.
+  griddep_wait();
+  if (MODE == MV_PCG && (batch ? P.bctl->all_done : P.sc->done)) {
+    if (threadIdx.x == 0)  // let the copies issued above land before the CTA exits
+      for (int k = 0; k < 2; ++k)
+        if (blockIdx.x + k * step < P.n_patches) mbar_wait_bounded(&bar[k], 0u);
+    return;
+  }
+  T beta = 0;
+  if (MODE == MV_PCG && !batch) beta = T(P.sc->beta);
   // gathers of the node vectors of the patch in buffer Bq into stage st
   auto issue_gathers = [&](const unsigned char *Bq, T *st) {
     const int32_t *nq = reinterpret_cast<const int32_t *>(Bq + L.nodes_off);
@@ -552,6 +560,7 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
       }
     }
   }
+  griddep_launch_dependents();
   if (MODE == MV_PCG && !batch) {
     DotAcc<T> ea[1] = {energy};
     double v[1];

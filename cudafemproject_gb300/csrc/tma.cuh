@@ -32,6 +32,14 @@ __device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned b
                : "memory");
 }
 
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialization may start while its predecessor in the stream runs. It must
+// call griddep_wait() before it reads anything the predecessor writes;
+// griddep_launch_dependents() lets the next such kernel start early. Both are
+// no-ops for kernels launched without the attribute.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // 16-byte asynchronous copy global -> shared (L2 only), completed by cp_async_wait.
 __device__ __forceinline__ void cp_async16(void *dst, const void *src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
