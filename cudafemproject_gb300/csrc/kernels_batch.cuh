@@ -37,7 +37,8 @@ __global__ void __launch_bounds__(kThreads) k_batch_vec(BatchVecParams<T> P, T *
     const Scalars &s = P.isc[inst];
     DotAcc<T> acc[3];
     const bool frozen = !init && s.done;
-    if (!frozen) {
+    if (frozen) continue;  // (uniform per CTA) its instance's sums are no longer read
+    {
       const T alpha = init ? T(0) : (T)s.alpha;
       for (int n = P.own_first[patch] + threadIdx.x; n < P.own_first[patch + 1]; n += blockDim.x) {
         NodeV<T, VW> zero;

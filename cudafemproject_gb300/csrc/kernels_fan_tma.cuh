@@ -218,28 +218,47 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
   }
   __syncthreads();
   const int step = gridDim.x;
-  if (threadIdx.x == 0) {
-    for (int k = 0; k < 2; ++k) {
-      const int q = blockIdx.x + k * step;
-      if (q < P.n_patches) {
-        mbar_expect_tx(&bar[k], (unsigned)L.bytes);
-        if (F.evict_first)
-          bulk_load_hint(k ? buf1 : buf0, F.blocks + (size_t)q * L.bytes, (unsigned)L.bytes, &bar[k],
-                         l2_evict_first_policy());
-        else
-          bulk_load(k ? buf1 : buf0, F.blocks + (size_t)q * L.bytes, (unsigned)L.bytes, &bar[k]);
-      }
-    }
-  }
-  // The first two blocks (static operator data) are on their way; everything
-  // below reads what the previous kernel in the stream wrote.
+  // Batched PCG: patches of converged instances are skipped, and their blocks
+  // are not copied at all (the convergence flags come from the previous
+  // kernel; up to kDoneCache instances they are cached in shared memory).
+  // Every other patch is live.
+  constexpr int kDoneCache = 256;  // (static shared memory of the kernel must stay small: 3 CTAs per SM)
+  __shared__ unsigned char inst_done[kDoneCache];
+  auto patch_live = [&](int q) -> bool {
+    if (!(batch && MODE == MV_PCG)) return true;
+    const int i = P.patch_inst[q];
+    return i < kDoneCache ? inst_done[i] == 0 : P.isc[i].done == 0;
+  };
+  auto issue_copy = [&](int q, int k) {  // block of patch q into buffer k
+    mbar_expect_tx(&bar[k], (unsigned)L.bytes);
+    if (F.evict_first)
+      bulk_load_hint(k ? buf1 : buf0, F.blocks + (size_t)q * L.bytes, (unsigned)L.bytes, &bar[k],
+                     l2_evict_first_policy());
+    else
+      bulk_load(k ? buf1 : buf0, F.blocks + (size_t)q * L.bytes, (unsigned)L.bytes, &bar[k]);
+  };
+  // Single mesh: the first two blocks (static operator data) are on their way
+  // before the wait for the previous kernel; everything below reads what that
+  // kernel wrote.
+  if (threadIdx.x == 0 && !batch)
+    for (int k = 0; k < 2; ++k)
+      if (blockIdx.x + k * step < P.n_patches) issue_copy(blockIdx.x + k * step, k);
   griddep_wait();
   if (MODE == MV_PCG && (batch ? P.bctl->all_done : P.sc->done)) {
-    if (threadIdx.x == 0)  // let the copies issued above land before the CTA exits
+    if (threadIdx.x == 0 && !batch)  // let the copies issued above land before the CTA exits
       for (int k = 0; k < 2; ++k)
         if (blockIdx.x + k * step < P.n_patches) mbar_wait_bounded(&bar[k], 0u);
     return;
   }
+  if (batch && MODE == MV_PCG) {
+    for (int i = threadIdx.x; i < P.n_inst && i < kDoneCache; i += blockDim.x) inst_done[i] = P.isc[i].done != 0;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && batch)
+    for (int k = 0; k < 2; ++k)
+      if (blockIdx.x + k * step < P.n_patches && patch_live(blockIdx.x + k * step))
+        issue_copy(blockIdx.x + k * step, k);
+  unsigned phase = 0;  // bit b: parity of the next completion of buffer b's barrier
   T beta = 0;
   if (MODE == MV_PCG && !batch) beta = T(P.sc->beta);
   // gathers of the node vectors of the patch in buffer Bq into stage st
@@ -264,12 +283,18 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
     // Every thread waits for the block itself; the staging barrier below
     // makes a failed copy a uniform exit (a thread whose wait failed reads
     // nothing of the block before it).
-    const bool ok = mbar_wait_bounded(&bar[b], (unsigned)((it >> 1) & 1));
+    const bool live = patch_live(patch);
+    bool ok = true;
+    if (live) {
+      ok = mbar_wait_bounded(&bar[b], (phase >> b) & 1u);
+      phase ^= 1u << b;
+    }
     auto copy_failed = [&]() {
       if (PREFETCH) cp_async_wait<0>();
       if (threadIdx.x == 0) {
         atomicOr(F.err, kErrTmaTimeout);
-        if (patch + step < P.n_patches) mbar_wait_bounded(&bar[b ^ 1], (unsigned)(((it + 1) >> 1) & 1));
+        if (patch + step < P.n_patches && patch_live(patch + step))
+          mbar_wait_bounded(&bar[b ^ 1], (phase >> (b ^ 1)) & 1u);
       }
     };
     if (batch && __syncthreads_or(!ok)) {  // (uniform: batch is a kernel parameter)
@@ -286,9 +311,8 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
       lam = P.pmat[2 * patch];
       mu = P.pmat[2 * patch + 1];
       if (MODE == MV_PCG) {
-        const Scalars &si = P.isc[P.patch_inst[patch]];
-        skip = si.done != 0;
-        beta = T(si.beta);
+        skip = !live;
+        beta = T(P.isc[P.patch_inst[patch]].beta);
       }
     }
     if (!skip) {
@@ -482,8 +506,7 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
         stv<T, VW>(fs, half_fpos(B + L.fpos_off, threadIdx.x, k), o);
       }
     if constexpr (PREFETCH) {  // the next patch's gathers overlap the node sums below
-      if (patch + step < P.n_patches &&
-          mbar_wait_bounded(&bar[b ^ 1], (unsigned)(((it + 1) >> 1) & 1)))
+      if (patch + step < P.n_patches && mbar_wait_bounded(&bar[b ^ 1], (phase >> (b ^ 1)) & 1u))
         issue_gathers(b ? buf0 : buf1, sp + (size_t)((it + 1) & 1) * stage_stride);
       cp_async_commit();
     }
@@ -549,14 +572,7 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
       if (atomicAdd(&warps_done[b], 1u) == kHfanThreads / 32 - 1) {
         __threadfence_block();
         warps_done[b] = 0;
-        if (patch + 2 * step < P.n_patches) {
-          mbar_expect_tx(&bar[b], (unsigned)L.bytes);
-          const unsigned char *src = F.blocks + (size_t)(patch + 2 * step) * L.bytes;
-          if (F.evict_first)
-            bulk_load_hint(B, src, (unsigned)L.bytes, &bar[b], l2_evict_first_policy());
-          else
-            bulk_load(B, src, (unsigned)L.bytes, &bar[b]);
-        }
+        if (patch + 2 * step < P.n_patches && patch_live(patch + 2 * step)) issue_copy(patch + 2 * step, b);
       }
     }
   }
