@@ -388,18 +388,28 @@ struct MvParams {
 };
 
 // Last-block helper for batches: per instance i, the sum of vals[p*stride + k]
-// over its contiguous patch range, one warp per instance (strided lane sums
-// and a shuffle tree: a fixed order). Called by all threads of one block.
+// over its contiguous patch range, one warp per instance (each lane keeps four
+// interleaved partial sums so that its loads overlap, then a shuffle tree: a
+// fixed order). Instances with skip[i] != 0 (when skip is given) are left
+// out. Called by all threads of one block.
 template <int N>
 __device__ __forceinline__ void instance_sums(const double *vals, int stride, const int32_t *inst_patch_off, int n_inst,
-                                              double *out /* [n_inst][N] */) {
+                                              double *out /* [n_inst][N] */, const Scalars *skip = nullptr) {
   const int lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
   for (int i = threadIdx.x >> 5; i < n_inst; i += nwarp) {
+    if (skip && skip[i].done) continue;
     const int p0 = inst_patch_off[i], p1 = inst_patch_off[i + 1];
 #pragma unroll
     for (int k = 0; k < N; ++k) {
-      double s = 0;
-      for (int p = p0 + lane; p < p1; p += 32) s += __ldcg(vals + (size_t)p * stride + k);
+      double s4[4] = {0, 0, 0, 0};
+      int p = p0 + lane;
+      for (; p + 96 < p1; p += 128)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) s4[q] += __ldcg(vals + (size_t)(p + 32 * q) * stride + k);
+#pragma unroll
+      for (int q = 0; q < 3; ++q)
+        if (p + 32 * q < p1) s4[q] += __ldcg(vals + (size_t)(p + 32 * q) * stride + k);
+      double s = (s4[0] + s4[1]) + (s4[2] + s4[3]);
       for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
       if (lane == 0) out[(size_t)i * N + k] = s;
     }

@@ -90,7 +90,7 @@ __global__ void __launch_bounds__(kThreads) k_batch_vec(BatchVecParams<T> P, T *
   __syncthreads();
   if (!last) return;
   __threadfence();
-  instance_sums<3>(P.pp, 3, P.inst_patch_off, P.n_inst, P.scratch);
+  instance_sums<3>(P.pp, 3, P.inst_patch_off, P.n_inst, P.scratch, init ? nullptr : P.isc);
   __syncthreads();
   __shared__ int s_active;
   if (threadIdx.x == 0) s_active = 0;

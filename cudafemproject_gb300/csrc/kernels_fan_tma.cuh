@@ -592,7 +592,7 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
     __syncthreads();
     if (!last) return;
     __threadfence();
-    instance_sums<1>(P.patch_energy, 1, P.inst_patch_off, P.n_inst, P.partials);
+    instance_sums<1>(P.patch_energy, 1, P.inst_patch_off, P.n_inst, P.partials, P.isc);
     __syncthreads();
     for (int i = threadIdx.x; i < P.n_inst; i += blockDim.x) {
       Scalars &si = P.isc[i];
