@@ -39,24 +39,6 @@ MvParams<T> base_mv_t(cfem_ctx *c) {
   return P;
 }
 
-// Launch with programmatic stream serialization: the kernel may start while
-// the previous kernel in the stream runs (it calls griddep_wait before reading
-// that kernel's results). Used for the matvec / update pairs of the PCG loop.
-template <typename... KArgs, typename... Args>
-static void launch_pdl(void (*kern)(KArgs...), dim3 g, dim3 b, size_t smem, cudaStream_t s, Args... args) {
-  cudaLaunchConfig_t cfg{};
-  cfg.gridDim = g;
-  cfg.blockDim = b;
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = s;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  CK(cudaLaunchKernelEx(&cfg, kern, args...));
-}
-
 template <typename T>
 void launch_mv_t(cfem_ctx *c, int mode, const MvParams<T> &P) {
   if (c->n_inst && !P.patch_inst)
@@ -81,7 +63,7 @@ void launch_mv_t(cfem_ctx *c, int mode, const MvParams<T> &P) {
         dim3 g(c->grid_geo), b(kHfanThreads);
         if (mode == MV_PLAIN) k_matvec_fan_tma<float, MV_PLAIN, true><<<g, b, c->smem_geo, c->stream>>>(P, F);
         else if (mode == MV_PCG) launch_pdl(k_matvec_fan_tma<float, MV_PCG, true>, g, b, c->smem_geo, c->stream, P, F);
-        else k_matvec_fan_tma<float, MV_DYN, true><<<g, b, c->smem_geo, c->stream>>>(P, F);
+        else launch_pdl(k_matvec_fan_tma<float, MV_DYN, true>, g, b, c->smem_geo, c->stream, P, F);
         CKL();
         c->launches += 1;
         return;
@@ -89,7 +71,7 @@ void launch_mv_t(cfem_ctx *c, int mode, const MvParams<T> &P) {
       dim3 g(c->grid_ft32), b(kHfanThreads);
       if (mode == MV_PLAIN) k_matvec_fan_tma<float, MV_PLAIN><<<g, b, c->smem_ft32, c->stream>>>(P, F);
       else if (mode == MV_PCG) launch_pdl(k_matvec_fan_tma<float, MV_PCG>, g, b, c->smem_ft32, c->stream, P, F);
-      else k_matvec_fan_tma<float, MV_DYN><<<g, b, c->smem_ft32, c->stream>>>(P, F);
+      else launch_pdl(k_matvec_fan_tma<float, MV_DYN>, g, b, c->smem_ft32, c->stream, P, F);
       CKL();
       c->launches += 1;
       return;

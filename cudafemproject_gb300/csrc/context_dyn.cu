@@ -83,7 +83,7 @@ void set_pcg_vectors(cfem_ctx *c, const double *diag_op, const double *diag_pre)
 
 template <typename T>
 void launch_dyn_explicit(cfem_ctx *c, const DynParams<T> &P) {
-  if (c->dim == 3) k_dyn_explicit<T, 3><<<c->grid_vec, kThreads, 0, c->stream>>>(P);
+  if (c->dim == 3) launch_pdl(k_dyn_explicit<T, 3>, dim3(c->grid_vec), dim3(kThreads), 0, c->stream, P);
   else k_dyn_explicit<T, 2><<<c->grid_vec, kThreads, 0, c->stream>>>(P);
   CKL();
 }
@@ -235,8 +235,7 @@ cfem_status run_dyn(cfem_ctx *c, const cfem_dyn_params *prm, const cfem_wavelet 
         CKL();
       }
       launch_dyn_explicit<T>(c, dp);
-      if constexpr (sizeof(T) == 8) k_dyn_end_step<T><<<1, kThreads, 0, c->stream>>>(dp, to, c->vw);
-      else k_dyn_end_step<T><<<1, kThreads, 0, c->stream>>>(dp, to, c->vw);
+      launch_pdl(k_dyn_end_step<T>, dim3(1), dim3(kThreads), 0, c->stream, dp, (const T *)to, c->vw);
       CKL();
     }
   };

@@ -222,6 +222,27 @@ void make_rhs(cfem_ctx *c, double a, double b, double *dst);
 cfem_status run_guarded(const std::function<cfem_status()> &fn);
 void check_ctx(const cfem_ctx *c);
 // Throws if a bulk-copy wait of the edge-fan matvec timed out (synchronises the stream).
+// Launch with programmatic stream serialization: the kernel may start while
+// the previous kernel in the stream runs (it calls griddep_wait before reading
+// that kernel's results). Used for the matvec / update pairs of the PCG loop
+// and the kernels of an explicit dynamics step. Every kernel launched this
+// way waits for its predecessor before it finishes, so completion stays
+// ordered along the stream.
+template <typename... KArgs, typename... Args>
+inline void launch_pdl(void (*kern)(KArgs...), dim3 g, dim3 b, size_t smem, cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = g;
+  cfg.blockDim = b;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  CK(cudaLaunchKernelEx(&cfg, kern, args...));
+}
+
 void check_copy_error(cfem_ctx *c);
 // Orders the context's stream after the caller's stream (device inputs written there).
 void enter(cfem_ctx *c);

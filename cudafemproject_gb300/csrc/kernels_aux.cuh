@@ -216,6 +216,8 @@ struct DynParams {
 template <typename T, int DIM>
 __global__ void k_dyn_explicit(DynParams<T> P) {
   constexpr int VW = DIM == 3 ? 4 : 2;
+  griddep_wait();               // y from the step's matvec
+  griddep_launch_dependents();  // (the end-of-step kernel, then the next matvec)
   const int step = P.st->step;
   const T ca = (T)P.coef[2 * step], cb = (T)P.coef[2 * step + 1];
   for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < P.n_nodes; n += (int64_t)gridDim.x * blockDim.x) {
@@ -273,6 +275,8 @@ __global__ void k_dyn_correct(DynParams<T> P) {
 // Ends a step: records receiver displacements and advances the step counter.
 template <typename T>
 __global__ void k_dyn_end_step(DynParams<T> P, const T *d, int VW) {
+  griddep_wait();
+  griddep_launch_dependents();  // the next step's matvec starts streaming its blocks
   const int step = P.st->step;
   for (int i = threadIdx.x; i < P.n_recv * P.dim; i += blockDim.x) {
     int r = i / P.dim, k = i % P.dim;
