@@ -1,7 +1,7 @@
 """GPU parity of the static path against the oracle and the reference fixtures.
 
-Tolerances: FP64 paths <= 1e-10 relative to the converged FP64 oracle (the
-spec bound); FP32 + FP64 refinement <= 1e-8; FP32-only results are held
+Tolerances: FP64 paths <= 1e-10 relative to the converged FP64 oracle;
+FP32 + FP64 refinement <= 1e-8; FP32-only results are held
 to FP32 accuracy. DOF map, adjacency, constraint masks and renumbering are
 bit-exact.
 """
