@@ -144,8 +144,9 @@ MultiState &multi_state(cfem_ctx *c, int K) {
   M->active.alloc(K);
   CK(cudaMallocHost(&M->h_ctl, sizeof(MultiCtl)));
   M->h_sc.resize(K);
+  // four items per thread per round: two CTAs per SM keep enough loads in flight
   M->grid_vec = (int)std::min<int64_t>(std::max<int64_t>(1, (int64_t)(((size_t)c->nn * K + kThreads - 1) / kThreads)),
-                                       (int64_t)c->n_sm * 4);
+                                       (int64_t)c->n_sm * 2);
   const int max_mv_grid = c->n_sm * 8;
   M->partials.alloc((size_t)std::max(max_mv_grid, M->grid_vec) * K * 3);
   return *M;

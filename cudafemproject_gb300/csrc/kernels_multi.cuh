@@ -52,6 +52,49 @@ inline size_t multi_smem_bytes(const FanBlockLayout &L, int R) {
 // y_c += K' p_c for the K cases. PCG (MODE MV_PCG): p_c = z_c + beta_c p_old_c
 // staged on the fly (written back by the owning patch), sigma_c = p_c.K'p_c.
 // PLAIN: y_c += K' x_c. FP32 only (the patch blocks hold FP32 gradients).
+// Last-block helper: per case c < K the sums over the grid's blocks b of
+// partials[(b * K + c) * NQ + k], in a fixed order, into out[c * NQ + k].
+// Many cases: one thread per case with eight interleaved partial sums, so that
+// its loads overlap. Few cases: one warp per case, four interleaved partial
+// sums per lane and a shuffle tree. Called by all threads of the last block.
+template <int NQ>
+__device__ __forceinline__ void case_sums(const double *partials, int nblocks, int K, double *out) {
+  if (K >= 128) {
+    for (int c = threadIdx.x; c < K; c += blockDim.x) {
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) {
+        double s8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        int b = 0;
+        for (; b + 8 <= nblocks; b += 8)
+#pragma unroll
+          for (int q = 0; q < 8; ++q) s8[q] += __ldcg(partials + ((size_t)(b + q) * K + c) * NQ + k);
+#pragma unroll
+        for (int q = 0; q < 7; ++q)
+          if (b + q < nblocks) s8[q] += __ldcg(partials + ((size_t)(b + q) * K + c) * NQ + k);
+        out[c * NQ + k] = ((s8[0] + s8[1]) + (s8[2] + s8[3])) + ((s8[4] + s8[5]) + (s8[6] + s8[7]));
+      }
+    }
+    return;
+  }
+  const int lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
+  for (int c = threadIdx.x >> 5; c < K; c += nwarp) {
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) {
+      double s4[4] = {0, 0, 0, 0};
+      int b = lane;
+      for (; b + 96 < nblocks; b += 128)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) s4[q] += __ldcg(partials + ((size_t)(b + 32 * q) * K + c) * NQ + k);
+#pragma unroll
+      for (int q = 0; q < 3; ++q)
+        if (b + 32 * q < nblocks) s4[q] += __ldcg(partials + ((size_t)(b + 32 * q) * K + c) * NQ + k);
+      double t = (s4[0] + s4[1]) + (s4[2] + s4[3]);
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+      if (lane == 0) out[c * NQ + k] = t;
+    }
+  }
+}
+
 template <int MODE, int R>
 __global__ void __launch_bounds__(kHfanThreads) k_matvec_multi(MultiParams<float> P, const float *x, const float *pold,
                                                                float *pnew, float *y) {
@@ -267,9 +310,11 @@ __global__ void __launch_bounds__(kHfanThreads) k_matvec_multi(MultiParams<float
   __syncthreads();
   if (!last) return;
   __threadfence();
+  __shared__ double s_tot[kMaxCases];
+  case_sums<1>(P.partials, gridDim.x, K, s_tot);
+  __syncthreads();
   for (int c = threadIdx.x; c < K; c += blockDim.x) {
-    double t = 0;
-    for (int b = 0; b < (int)gridDim.x; ++b) t += __ldcg(P.partials + (size_t)b * K + c);
+    const double t = s_tot[c];
     MultiScalars &s = P.sc[c];
     s.sigma = t;
     s.alpha = s.done ? 0.0 : s.gamma / t;
@@ -293,43 +338,64 @@ __global__ void __launch_bounds__(kThreads) k_pcg_multi_vec(MultiParams<T> P, T 
   const T alpha = init || frozen ? T(0) : (T)s.alpha;
   DotAcc<T> acc[3];  // r.z, r.r, f.f
   const int64_t n_items = P.n_nodes * K;
-  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n_items; q += (int64_t)gridDim.x * blockDim.x) {
+  // U items per thread per round, all loads issued before any is used; the
+  // stride is a multiple of K, so every item of a thread is case c
+  constexpr int U = 4;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t q0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q0 < n_items; q0 += stride * U) {
     NodeV<T, VW> zero;
 #pragma unroll
     for (int d = 0; d < VW; ++d) zero.v[d] = 0;
     if (frozen) {
-      stv<T, VW>(u, q, zero);
+#pragma unroll
+      for (int k = 0; k < U; ++k)
+        if (q0 + k * stride < n_items) stv<T, VW>(u, q0 + k * stride, zero);
       continue;
     }
-    const NodeV<T, VW> di = ldv<T, VW>(dinv, q / K);
-    NodeV<T, VW> rv, xx, zz = zero;
-    if (init) {
-      rv = ldv<T, VW>(f, q);
-      xx = zero;
-    } else {
-      rv = ldv<T, VW>(r, q);
-      xx = ldv<T, VW>(xv, q);
-      const NodeV<T, VW> pp = ldv<T, VW>(p, q), uu = ldv<T, VW>(u, q);
+    NodeV<T, VW> di[U], rv[U], xx[U], pp[U], uu[U];
 #pragma unroll
-      for (int d = 0; d < DIM; ++d) {
-        xx.v[d] += alpha * pp.v[d];
-        rv.v[d] -= alpha * uu.v[d];
+    for (int k = 0; k < U; ++k) {
+      const int64_t q = q0 + k * stride;
+      if (q >= n_items) continue;
+      di[k] = ldv<T, VW>(dinv, q / K);
+      if (init) {
+        rv[k] = ldv<T, VW>(f, q);
+      } else {
+        rv[k] = ldv<T, VW>(r, q);
+        xx[k] = ldv<T, VW>(xv, q);
+        pp[k] = ldv<T, VW>(p, q);
+        uu[k] = ldv<T, VW>(u, q);
       }
     }
-    T rz = 0, rr = 0;
 #pragma unroll
-    for (int d = 0; d < DIM; ++d) {
-      zz.v[d] = rv.v[d] * di.v[d];
-      rz += rv.v[d] * zz.v[d];
-      rr += rv.v[d] * rv.v[d];
+    for (int k = 0; k < U; ++k) {
+      const int64_t q = q0 + k * stride;
+      if (q >= n_items) continue;
+      NodeV<T, VW> zz = zero;
+      if (init) {
+        xx[k] = zero;
+      } else {
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+          xx[k].v[d] += alpha * pp[k].v[d];
+          rv[k].v[d] -= alpha * uu[k].v[d];
+        }
+      }
+      T rz = 0, rr = 0;
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) {
+        zz.v[d] = rv[k].v[d] * di[k].v[d];
+        rz += rv[k].v[d] * zz.v[d];
+        rr += rv[k].v[d] * rv[k].v[d];
+      }
+      acc[0].add(rz);
+      acc[1].add(rr);
+      if (init) acc[2].add(rr);
+      stv<T, VW>(xv, q, xx[k]);
+      stv<T, VW>(r, q, rv[k]);
+      stv<T, VW>(z, q, zz);
+      stv<T, VW>(u, q, zero);
     }
-    acc[0].add(rz);
-    acc[1].add(rr);
-    if (init) acc[2].add(rr);
-    stv<T, VW>(xv, q, xx);
-    stv<T, VW>(r, q, rv);
-    stv<T, VW>(z, q, zz);
-    stv<T, VW>(u, q, zero);
   }
   // block partials per case: threads c, c + K, ... in order
   __shared__ double red[3][kThreads];
@@ -355,12 +421,11 @@ __global__ void __launch_bounds__(kThreads) k_pcg_multi_vec(MultiParams<T> P, T 
   __shared__ int s_active;
   if (threadIdx.x == 0) s_active = 0;
   __syncthreads();
+  double *s_tot = &red[0][0];  // [K][3] (K <= kThreads)
+  case_sums<3>(P.partials, gridDim.x, K, s_tot);
+  __syncthreads();
   for (int cc = threadIdx.x; cc < K; cc += blockDim.x) {
-    double a = 0, b = 0, e = 0;
-    for (int bb = 0; bb < (int)gridDim.x; ++bb) {
-      const double *pt = P.partials + ((size_t)bb * K + cc) * 3;
-      a += __ldcg(pt); b += __ldcg(pt + 1); e += __ldcg(pt + 2);
-    }
+    const double a = s_tot[cc * 3], b = s_tot[cc * 3 + 1], e = s_tot[cc * 3 + 2];
     MultiScalars &m = P.sc[cc];
     if (init) {
       m.gamma0 = m.gamma = m.gamma_prev = a;
