@@ -35,7 +35,8 @@
 namespace cfem {
 
 constexpr int kStageUnroll = 2;      // node gathers in flight per thread while staging a patch
-constexpr int kHalfSlots = 12;       // force slots per fan: 2 halves x (P, Q, 4 ring vertices)
+constexpr int kHalfSlots = 12;       // node slots per fan: 2 halves x (P, Q, 4 ring vertices)
+constexpr int kFanForces = 9;        // force-list entries per fan (the halves share P, Q and R_3)
 constexpr int kHfanThreads = 2 * kFanThreads;
 constexpr uint16_t kNoSlot = 0xFFFF;  // absent slot of a half-thread
 
@@ -142,7 +143,7 @@ inline FanBlockLayout fan_geo_block_layout(int np_max, bool with_scale) {
   return L;
 }
 
-constexpr int kForceBytes = 9 * kFanThreads * 16;  // separate force list of geometry blocks (9 entries per fan)
+constexpr int kForceBytes = kFanForces * kFanThreads * 16;  // separate force list of geometry blocks
 
 // Geometry blocks: two buffers, the force list, and two stages of the node
 // vectors a PCG-form matvec reads (z and p_old), gathered one patch ahead.
@@ -198,7 +199,7 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
   const FanBlockLayout &L = F.L;
   unsigned char *buf0 = smem_raw, *buf1 = smem_raw + L.bytes;
   unsigned char *tail = smem_raw + 2 * (size_t)L.bytes;
-  T *fgeo = reinterpret_cast<T *>(tail);                          // GEO: [kHalfSlots x kFanThreads][4] forces
+  T *fgeo = reinterpret_cast<T *>(tail);                          // GEO: [kFanForces x kFanThreads][4] forces
   if (GEO) tail += kForceBytes;
   T *sp = reinterpret_cast<T *>(tail);                            // [npn][4] staged node values
   // GEO: [2 stages][z, p_old][npn][4] (PCG form; the other modes use stage 0 as sp)

@@ -44,14 +44,11 @@ struct MultiParams {
 
 // Shared memory of k_matvec_multi: one patch block, R force lists, R staged node blocks.
 inline size_t multi_smem_bytes(const FanBlockLayout &L, int R) {
-  const int fs_bytes = kHalfSlots * kFanThreads * 4 * (int)sizeof(float);
+  const int fs_bytes = kFanForces * kFanThreads * 4 * (int)sizeof(float);
   return (size_t)L.bytes + (size_t)R * fs_bytes + (size_t)R * L.npn * 4 * sizeof(float) + 16 +
          (size_t)kMaxCases * sizeof(double) + 64;
 }
 
-// y_c += K' p_c for the K cases. PCG (MODE MV_PCG): p_c = z_c + beta_c p_old_c
-// staged on the fly (written back by the owning patch), sigma_c = p_c.K'p_c.
-// PLAIN: y_c += K' x_c. FP32 only (the patch blocks hold FP32 gradients).
 // Last-block helper: per case c < K the sums over the grid's blocks b of
 // partials[(b * K + c) * NQ + k], in a fixed order, into out[c * NQ + k].
 // Many cases: one thread per case with eight interleaved partial sums, so that
@@ -95,6 +92,9 @@ __device__ __forceinline__ void case_sums(const double *partials, int nblocks, i
   }
 }
 
+// y_c += K' p_c for the K cases. PCG (MODE MV_PCG): p_c = z_c + beta_c p_old_c
+// staged on the fly (written back by the owning patch), sigma_c = p_c.K'p_c.
+// PLAIN: y_c += K' x_c. FP32 only (the patch blocks hold FP32 gradients).
 template <int MODE, int R>
 __global__ void __launch_bounds__(kHfanThreads) k_matvec_multi(MultiParams<float> P, const float *x, const float *pold,
                                                                float *pnew, float *y) {
@@ -105,8 +105,8 @@ __global__ void __launch_bounds__(kHfanThreads) k_matvec_multi(MultiParams<float
   const int K = P.K;
   unsigned char *B = smem_raw;
   // case-fastest layouts: the R cases of one node (or force slot) are adjacent
-  T *fs = reinterpret_cast<T *>(smem_raw + L.bytes);                            // [kHalfSlots * kFanThreads][R][4]
-  constexpr int FS = kHalfSlots * kFanThreads * VW;
+  T *fs = reinterpret_cast<T *>(smem_raw + L.bytes);                            // [kFanForces * kFanThreads][R][4]
+  constexpr int FS = kFanForces * kFanThreads * VW;
   T *sp = fs + (size_t)R * FS;                                                  // [npn][R][4]
   uint64_t *bar = reinterpret_cast<uint64_t *>(sp + (size_t)R * L.npn * VW);
   double *s_en = reinterpret_cast<double *>(bar + 2);                           // [K] energies of this block
