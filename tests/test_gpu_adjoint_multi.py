@@ -156,3 +156,19 @@ def test_explicit_dynamics_adjoint_checkpointed():
             vals.append(Lq)
         fd = (vals[0] - vals[1]) / (2e-4 * E[e])
         assert abs(fd - g[e]) <= 1e-4 * abs(g[e]), (e, fd, g[e])
+
+
+def test_multi_rhs_many_cases():
+    """130 load cases (padded to 256): the per-case grid sums take their
+    thread-per-case form; cases still match the FP64 oracle."""
+    from cudafemproject_gb300.solver import FemContext
+    p = meshgen.box_3d(4, 4, 12, jitter=0.2, seed=6)
+    o = O.Oracle(p)
+    rng = np.random.default_rng(13)
+    F = rng.standard_normal((130, p.n_dof)) * 10.0 ** rng.uniform(2, 4, size=(130, 1))
+    ctx = FemContext(p)
+    U, infos = ctx.pcg_multi(F, precision="fp32_refine", tol=1e-4, stop_rule="residual", outer_tol=1e-12)
+    for i in (0, 64, 129):
+        x, _ = o.pcg(F[i], tol=1e-14, rule=1)
+        assert rel(U[i], x) <= 1e-8, i
+        assert infos[i]["status"] == 0
