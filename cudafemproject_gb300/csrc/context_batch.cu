@@ -19,7 +19,7 @@ namespace {
 struct BatchBufs {
   DBuf<Scalars> isc;
   DBuf<BatchCtl> ctl;
-  DBuf<double> pe, pp, scratch, rrff;
+  DBuf<double> pe, pp, scratch, rrff, seg;
   DBuf<int> active;
 };
 
@@ -51,6 +51,9 @@ void batch_mv(cfem_ctx *c, BatchBufs &B, MvParams<T> &mv) {
 }
 
 int vec_grid(cfem_ctx *c) { return (int)std::min<int64_t>(c->prep.n_patches, (int64_t)c->n_sm * 8); }
+// flat vector step (k_batch_vec_flat): two CTAs per SM, four nodes in flight per thread
+int flat_grid(cfem_ctx *c) { return c->n_sm * 2; }
+size_t flat_smem(cfem_ctx *c) { return (size_t)(4 * c->n_inst + 2) * sizeof(int); }
 
 // FP32 PCG of every instance on c->v32.f; instances with a zero right-hand
 // side are done at once. Per-instance results are returned in out.
@@ -66,8 +69,10 @@ void run_batch_pcg(cfem_ctx *c, BatchBufs &B, double tol, int rule, int maxit, s
   B.ctl.zero(c->stream);
   Vecs<float> &V = c->v32;
   BatchVecParams<float> vp = vec_params_batch<float>(c, B, c->n_inst);
-  const int gv = vec_grid(c);
-  k_batch_vec<float><<<gv, kThreads, 0, c->stream>>>(vp, V.x.p, V.r.p, V.z.p, nullptr, V.u.p, V.f.p, V.dinv.p, 1);
+  const int gv = flat_grid(c);
+  const size_t sv = flat_smem(c);
+  vp.seg = B.seg.p;
+  k_batch_vec_flat<float><<<gv, kThreads, sv, c->stream>>>(vp, V.x.p, V.r.p, V.z.p, nullptr, V.u.p, V.f.p, V.dinv.p, 1);
   CKL();
   c->launches += 1;
   MvParams<float> mv = base_mv<float>(c);
@@ -87,7 +92,7 @@ void run_batch_pcg(cfem_ctx *c, BatchBufs &B, double tol, int rule, int maxit, s
       m.xout = pnew;
       m.y = V.u.p;
       launch_mv<float>(c, MV_PCG, m);
-      k_batch_vec<float><<<gv, kThreads, 0, c->stream>>>(vp, V.x.p, V.r.p, V.z.p, pnew, V.u.p, V.f.p, V.dinv.p, 0);
+      k_batch_vec_flat<float><<<gv, kThreads, sv, c->stream>>>(vp, V.x.p, V.r.p, V.z.p, pnew, V.u.p, V.f.p, V.dinv.p, 0);
       CKL();
     }
   } catch (...) {
@@ -273,6 +278,10 @@ extern "C" cfem_status cfem_batch_static_solve(cfem_ctx *ctx, const cfem_solve_p
     B.ctl.alloc(1);
     B.pe.alloc(c->prep.n_patches);
     B.pp.alloc((size_t)c->prep.n_patches * 3);
+    B.seg.alloc((size_t)flat_grid(c) * n * 3);
+    if (flat_smem(c) > 48 * 1024)
+      CK(cudaFuncSetAttribute((const void *)k_batch_vec_flat<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)flat_smem(c)));
     B.scratch.alloc((size_t)n * 3);
     B.rrff.alloc((size_t)n * 2);
     B.active.alloc(n);
