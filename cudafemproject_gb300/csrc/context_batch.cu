@@ -178,6 +178,9 @@ extern "C" cfem_status cfem_create_batch(cfem_ctx **out, int32_t n, const cfem_m
                                          const cfem_material *mats, const cfem_options *opt, void *stream) {
   return run_guarded([&]() -> cfem_status {
     if (!out || !meshes || !mats || n <= 0) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "bad batch arguments"};
+    // the vector step keeps four ints per instance in shared memory
+    if (n > kMaxBatchInstances)
+      throw Fail{CFEM_ERR_INVALID_ARGUMENT, "at most " + std::to_string(kMaxBatchInstances) + " meshes per batch"};
     *out = nullptr;
     cfem_mesh all{};
     all.dim = 3;

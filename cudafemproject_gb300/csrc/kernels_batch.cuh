@@ -13,6 +13,8 @@
 
 namespace cfem {
 
+constexpr int kMaxBatchInstances = 8192;  // k_batch_vec_flat: 4 n + 2 ints of shared memory
+
 template <typename T>
 struct BatchVecParams {
   int n_patches, n_inst;

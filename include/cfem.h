@@ -231,6 +231,7 @@ CFEM_API cfem_status cfem_run_task(const char *config_path, const char *task, in
  * structural queries accept such a context; CFEM_ERR_UNSUPPORTED otherwise. */
 CFEM_API cfem_status cfem_create_batch(cfem_ctx **out, int32_t n, const cfem_mesh *meshes, const cfem_material *mats,
                                        const cfem_options *opt, void *stream);
+/* (n <= 8192 instances) */
 /* n instances; node_off / elem_off (may be NULL) receive n + 1 offsets into
  * the concatenated caller order. */
 CFEM_API cfem_status cfem_batch_info(const cfem_ctx *ctx, int32_t *n, int64_t *node_off, int64_t *elem_off);
