@@ -30,7 +30,7 @@ NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xco
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-ffp-contract=off", "-I", os.path.join(REPO, "include")]
 
 CU_SOURCES = ["context.cu", "context_dyn.cu", "context_multi.cu", "context_batch.cu"]
-CXX_SOURCES = ["prep.cpp", "femfunc.cpp"]
+CXX_SOURCES = ["prep.cpp", "femfunc.cpp", "kfile.cpp"]
 
 
 def _nvcc() -> str:

@@ -89,6 +89,10 @@ SIGNATURES = [
     ("cfem_pcg_multi", i32, [vp, C.POINTER(SolveParams), i32, vp, vp, C.POINTER(SolveInfo)]),
     ("cfem_autotune_patch_elems", i32, [C.POINTER(Mesh), C.POINTER(Material), C.POINTER(Options), vp, i32,
                                         C.POINTER(i32), vp]),
+    ("cfem_kfile_read", i32, [C.c_char_p, i32, C.POINTER(vp)]),
+    ("cfem_kfile_sizes", i32, [vp, vp, vp, vp, vp, vp]),
+    ("cfem_kfile_get", i32, [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+    ("cfem_kfile_free", None, [vp]),
     ("cfem_create_batch", i32, [C.POINTER(vp), i32, C.POINTER(Mesh), C.POINTER(Material), C.POINTER(Options), vp]),
     ("cfem_batch_info", i32, [vp, C.POINTER(i32), vp, vp]),
     ("cfem_batch_static_solve", i32, [vp, C.POINTER(SolveParams), vp, C.POINTER(SolveInfo)]),

@@ -29,6 +29,11 @@ for the reference load here unchanged:
 Where the reference would write a malformed file (an SPC set whose flags are
 all zero, a load or segment naming a curve that does not exist) this reader
 raises ``ValueError`` instead.
+
+``read_k`` runs the library's C++ reader (csrc/kfile.cpp, the same rules; one
+pass and hash maps, so multi-million-element meshes read in seconds); the
+Python statement below it is kept as its readable counterpart and is compared
+with it in the tests.
 """
 from __future__ import annotations
 
@@ -58,8 +63,13 @@ def _blocks(path: str):
     return out
 
 
-def read_k(path: str, dim: int, E: float = 2e7, nu: float = 0.3, rho: float = 2400.0) -> Problem:
-    """Parse a keyword file into a Problem (prepared-mesh content, FP64 values)."""
+def read_k(path: str, dim: int, E: float = 2e7, nu: float = 0.3, rho: float = 2400.0, native: bool = True) -> Problem:
+    """Parse a keyword file into a Problem (prepared-mesh content, FP64 values).
+
+    native: the library's C++ reader (cfem_kfile_read, linear in the file
+    size); False runs the Python statement of the same rules below."""
+    if native:
+        return _read_k_native(path, dim, E, nu, rho)
     node_ids: List[str] = []
     coords: List[List[float]] = []
     elems_raw: List[List[str]] = []
@@ -158,6 +168,37 @@ def read_k(path: str, dim: int, E: float = 2e7, nu: float = 0.3, rho: float = 24
                    face_nodes=np.array(fnodes, dtype=np.int32).reshape(-1, dim + 1),
                    face_elem=np.array(felem, dtype=np.int32), face_normal=np.array(fnorm).reshape(-1, dim),
                    face_pressure=np.array(fpress, dtype=np.float64), E=E, nu=nu, rho=rho)
+
+
+def _read_k_native(path: str, dim: int, E: float, nu: float, rho: float) -> Problem:
+    import ctypes as C
+    from . import capi
+    L = capi.lib()
+    h = C.c_void_p()
+    st = L.cfem_kfile_read(os.fsencode(path), int(dim), C.byref(h))
+    if st == capi.ERR_MESH:  # a malformed file: as the Python reader reports it
+        raise ValueError(L.cfem_last_error_string().decode(errors="replace"))
+    capi.check(st, "cfem_kfile_read")
+    try:
+        n = [C.c_int64() for _ in range(5)]
+        capi.check(L.cfem_kfile_sizes(h, *[C.byref(v) for v in n]), "cfem_kfile_sizes")
+        nn, ne, nc, nl, nf = (v.value for v in n)
+        nodes = np.zeros((nn, dim), np.float64)
+        elems = np.zeros((ne, dim + 1), np.int32)
+        cons = np.zeros((nc, 2), np.int32)
+        load_node = np.zeros(nl, np.int32)
+        load_vec = np.zeros((nl, dim), np.float64)
+        face_nodes = np.zeros((nf, dim + 1), np.int32)
+        face_elem = np.zeros(nf, np.int32)
+        face_normal = np.zeros((nf, dim), np.float64)
+        face_pressure = np.zeros(nf, np.float64)
+        arrs = (nodes, elems, cons, load_node, load_vec, face_nodes, face_elem, face_normal, face_pressure)
+        capi.check(L.cfem_kfile_get(h, *[a.ctypes.data for a in arrs]), "cfem_kfile_get")
+    finally:
+        L.cfem_kfile_free(h)
+    return Problem(dim=dim, nodes=nodes, elems=elems, cons=cons, load_node=load_node, load_vec=load_vec,
+                   face_nodes=face_nodes, face_elem=face_elem, face_normal=face_normal,
+                   face_pressure=face_pressure, E=E, nu=nu, rho=rho)
 
 
 def convert(k_path: str, prepared_dir: str, dim: int) -> Problem:

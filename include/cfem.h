@@ -229,6 +229,24 @@ CFEM_API cfem_status cfem_run_task(const char *config_path, const char *task, in
  * own (0-based per mesh); the batch concatenates them instance after instance
  * (cfem_batch_info gives the offsets). Only cfem_batch_static_solve and the
  * structural queries accept such a context; CFEM_ERR_UNSUPPORTED otherwise. */
+/* ---- LS-DYNA keyword (.k) meshes (host only, no GPU) --------------------
+ * The reference's converter (mesh_parser_lib/parser_src/parser_lib.py:36-378)
+ * turns a keyword file into the prepared-mesh files; cfem_kfile_read reads the
+ * same content into arrays: nodes [n][dim] (file order), elements [e][dim+1]
+ * (0-based node positions), constraints [c][2] (node, constraint code),
+ * nodal loads (node, [dim] vector), pressure faces ([dim+1]: the face's nodes,
+ * then the element's remaining node; element; normal [dim], not normalised,
+ * pointing away from the element; pressure). */
+typedef struct cfem_kfile cfem_kfile;
+CFEM_API cfem_status cfem_kfile_read(const char *path, int32_t dim, cfem_kfile **out);
+CFEM_API cfem_status cfem_kfile_sizes(const cfem_kfile *k, int64_t *n_nodes, int64_t *n_elems, int64_t *n_constraints,
+                                      int64_t *n_loads, int64_t *n_faces);
+/* Copies the arrays into caller buffers sized by cfem_kfile_sizes (NULL skips one). */
+CFEM_API cfem_status cfem_kfile_get(const cfem_kfile *k, double *nodes, int32_t *elems, int32_t *constraints,
+                                    int32_t *load_nodes, double *load_vectors, int32_t *face_nodes, int32_t *face_elems,
+                                    double *face_normals, double *face_pressures);
+CFEM_API void cfem_kfile_free(cfem_kfile *k);
+
 CFEM_API cfem_status cfem_create_batch(cfem_ctx **out, int32_t n, const cfem_mesh *meshes, const cfem_material *mats,
                                        const cfem_options *opt, void *stream);
 /* (n <= 8192 instances) */

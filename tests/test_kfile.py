@@ -49,3 +49,38 @@ def test_spc_without_dofs_is_rejected(tmp_path):
                     "*BOUNDARY_SPC_SET\n1 0 0 0 0\n*SET_NODE_LIST\n1\n1 2\n*END\n")
     with pytest.raises(ValueError):
         kfile.read_k(str(path), 2)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_native_reader_matches_python_statement(tmp_path, dim):
+    """The C++ reader (cfem_kfile_read) and the Python statement of the same
+    rules give identical arrays, on written meshes and, when present, on the
+    reference's raw meshes."""
+    paths = []
+    if dim == 3:
+        p = meshgen.box_3d(4, 3, 6, jitter=0.2, seed=2, traction=(0.0, -1e3, 0.0))
+    else:
+        p = meshgen.square_2d(9, traction=1e3)
+    path = str(tmp_path / f"m{dim}.k")
+    kfile.write_k(p, path)
+    paths.append(path)
+    raw_dir = os.path.join(os.path.dirname(REF_RAW), f"{dim}D")
+    if os.path.isdir(raw_dir):
+        small = sorted((os.path.getsize(os.path.join(raw_dir, f)), f) for f in os.listdir(raw_dir) if f.endswith(".k"))
+        paths += [os.path.join(raw_dir, f) for _, f in small[:4]]
+    for path in paths:
+        a = kfile.read_k(path, dim, native=True)
+        b = kfile.read_k(path, dim, native=False)
+        for f in ("nodes", "elems", "cons", "load_node", "load_vec", "face_nodes", "face_elem", "face_normal",
+                  "face_pressure"):
+            x, y = getattr(a, f), getattr(b, f)
+            assert x.shape == y.shape and np.array_equal(x, y), (path, f)
+
+
+def test_native_reader_rejects_bad_files(tmp_path):
+    path = tmp_path / "bad.k"
+    path.write_text("*NODE\n$\n1 0 0\n2 1 0\n$\n*ELEMENT_SHELL\n1 1 1 2 9 9\n*END\n")
+    with pytest.raises(ValueError):
+        kfile.read_k(str(path), 2)
+    with pytest.raises(Exception):
+        kfile.read_k(str(tmp_path / "missing.k"), 2)
