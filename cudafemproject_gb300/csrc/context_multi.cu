@@ -15,13 +15,14 @@ namespace cfem {
 namespace detail {
 
 struct MultiState {
-  int K = 0, R = 0;
+  int K = 0, C = 0;  // cases per solve (power of two), cases per matvec item
   DBuf<float> x, r, z, pA, pB, u, f;  // [node][K][4]
   DBuf<double> x64, f64, r64, io;     // [node][K][4]; io: caller-order staging
   DBuf<double> s_f, s_x, s_r;         // one case in the single-RHS layout
   DBuf<MultiScalars> sc;
   DBuf<MultiCtl> ctl;
-  DBuf<double> partials;
+  DBuf<double> partials, gpart;
+  DBuf<unsigned> gcnt;  // group tickets: [0, n) matvec, [n, 2n) vector kernel
   DBuf<int> active;
   MultiCtl *h_ctl = nullptr;
   std::vector<MultiScalars> h_sc;
@@ -38,27 +39,31 @@ void destroy_multi(MultiState *m) { delete m; }
 
 namespace {
 
-template <int R>
+template <int C>
 void launch_mvm(cfem_ctx *c, MultiState &M, int mode, const MultiParams<float> &P, const float *x, const float *pold,
                 float *pnew, float *y) {
   dim3 g(M.grid_mv), b(kHfanThreads);
-  if (mode == MV_PCG) k_matvec_multi<MV_PCG, R><<<g, b, M.smem, c->stream>>>(P, x, pold, pnew, y);
-  else k_matvec_multi<MV_PLAIN, R><<<g, b, M.smem, c->stream>>>(P, x, pold, pnew, y);
+  if (mode == MV_PCG) k_matvec_multi<MV_PCG, C><<<g, b, M.smem, c->stream>>>(P, x, pold, pnew, y);
+  else k_matvec_multi<MV_PLAIN, C><<<g, b, M.smem, c->stream>>>(P, x, pold, pnew, y);
   CKL();
   c->launches += 1;
 }
 
-void launch_mvm_r(cfem_ctx *c, MultiState &M, int mode, const MultiParams<float> &P, const float *x,
+void launch_mvm_c(cfem_ctx *c, MultiState &M, int mode, const MultiParams<float> &P, const float *x,
                   const float *pold, float *pnew, float *y) {
-  if (M.R == 1) launch_mvm<1>(c, M, mode, P, x, pold, pnew, y);
-  else if (M.R == 2) launch_mvm<2>(c, M, mode, P, x, pold, pnew, y);
-  else launch_mvm<4>(c, M, mode, P, x, pold, pnew, y);
+  if (M.C == 2) launch_mvm<2>(c, M, mode, P, x, pold, pnew, y);
+  else if (M.C == 4) launch_mvm<4>(c, M, mode, P, x, pold, pnew, y);
+  else if (M.C == 8) launch_mvm<8>(c, M, mode, P, x, pold, pnew, y);
+  else launch_mvm<16>(c, M, mode, P, x, pold, pnew, y);
 }
 
-const void *mvm_kernel(int R, int mode) {
-  if (R == 1) return mode == MV_PCG ? (const void *)k_matvec_multi<MV_PCG, 1> : (const void *)k_matvec_multi<MV_PLAIN, 1>;
-  if (R == 2) return mode == MV_PCG ? (const void *)k_matvec_multi<MV_PCG, 2> : (const void *)k_matvec_multi<MV_PLAIN, 2>;
-  return mode == MV_PCG ? (const void *)k_matvec_multi<MV_PCG, 4> : (const void *)k_matvec_multi<MV_PLAIN, 4>;
+template <int C>
+const void *mvm_kernel_c(int mode) {
+  return mode == MV_PCG ? (const void *)k_matvec_multi<MV_PCG, C> : (const void *)k_matvec_multi<MV_PLAIN, C>;
+}
+const void *mvm_kernel(int C, int mode) {
+  return C == 2 ? mvm_kernel_c<2>(mode) : C == 4 ? mvm_kernel_c<4>(mode) : C == 8 ? mvm_kernel_c<8>(mode)
+                                                                                  : mvm_kernel_c<16>(mode);
 }
 
 MultiParams<float> multi_params(cfem_ctx *c, MultiState &M) {
@@ -74,6 +79,9 @@ MultiParams<float> multi_params(cfem_ctx *c, MultiState &M) {
   P.sc = M.sc.p;
   P.ctl = M.ctl.p;
   P.partials = M.partials.p;
+  P.gpart = M.gpart.p;
+  P.gcnt_mv = M.gcnt.p;
+  P.gcnt_up = M.gcnt.p + M.gcnt.n / 2;
   P.F.blocks = c->blk32.p;
   P.F.L = c->L32;
   P.F.fan_off = c->fan_off.p;
@@ -82,45 +90,50 @@ MultiParams<float> multi_params(cfem_ctx *c, MultiState &M) {
   return P;
 }
 
-// Sets the launch shape for R cases per thread.
-void configure_r(cfem_ctx *c, MultiState &M, int R) {
+// Sets the launch shape for items of C cases; false if they do not fit in
+// shared memory.
+bool configure_c(cfem_ctx *c, MultiState &M, int C) {
   int optin = 0;
   CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
-  M.R = R;
-  M.smem = multi_smem_bytes(c->L32, R);
-  if (M.smem + 8192 > (size_t)optin) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "multi-RHS patch too large for shared memory"};
+  const size_t smem = (size_t)multi_smem(c->L32, C, M.K).bytes;
+  if (smem + 1024 > (size_t)optin) return false;  // (+ the kernel's static shared memory)
+  M.C = C;
+  M.smem = smem;
   for (int mode : {MV_PLAIN, MV_PCG})
-    CK(cudaFuncSetAttribute(mvm_kernel(R, mode), cudaFuncAttributeMaxDynamicSharedMemorySize, optin - 8192));
+    CK(cudaFuncSetAttribute(mvm_kernel(C, mode), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int occ = 1;
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, mvm_kernel(R, MV_PCG), kHfanThreads, M.smem));
-  M.grid_mv = (int)std::min<int64_t>(c->prep.n_patches, (int64_t)c->n_sm * std::max(occ, 1));
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, mvm_kernel(C, MV_PCG), kHfanThreads, M.smem));
+  const int64_t items = (int64_t)c->prep.n_patches * (M.K / C);
+  M.grid_mv = (int)std::min<int64_t>(items, (int64_t)c->n_sm * std::max(occ, 1));
   if (M.graph) {
     cudaGraphExecDestroy(M.graph);
     M.graph = nullptr;
   }
+  return true;
 }
 
-// Cases per thread: the variant with the shortest matvec on this mesh and
+// Cases per item: the variant with the shortest matvec on this mesh and
 // batch size, timed on the context's stream (PLAIN form, current vectors).
-void autotune_r(cfem_ctx *c, MultiState &M) {
+void autotune_c(cfem_ctx *c, MultiState &M) {
   float best = 1e30f;
-  int best_r = 1;
-  for (int R : {1, 2, 4}) {
-    if (R > M.K) break;
-    configure_r(c, M, R);
+  int best_c = 0;
+  for (int C : {2, 4, 8, 16}) {
+    if (C > M.K) break;
+    if (!configure_c(c, M, C)) continue;
     MultiParams<float> P = multi_params(c, M);
-    launch_mvm_r(c, M, MV_PLAIN, P, M.f.p, nullptr, nullptr, M.u.p);  // warm-up
+    launch_mvm_c(c, M, MV_PLAIN, P, M.f.p, nullptr, nullptr, M.u.p);  // warm-up
     CK(cudaEventRecord(c->ev0, c->stream));
-    for (int i = 0; i < 3; ++i) launch_mvm_r(c, M, MV_PLAIN, P, M.f.p, nullptr, nullptr, M.u.p);
+    for (int i = 0; i < 3; ++i) launch_mvm_c(c, M, MV_PLAIN, P, M.f.p, nullptr, nullptr, M.u.p);
     CK(cudaEventRecord(c->ev1, c->stream));
     CK(cudaEventSynchronize(c->ev1));
     float ms = 0;
     CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
-    if (ms < best) { best = ms; best_r = R; }
+    if (ms < best) { best = ms; best_c = C; }
   }
-  configure_r(c, M, best_r);
+  if (!best_c) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "multi-RHS patch too large for shared memory"};
+  configure_c(c, M, best_c);
   M.u.zero(c->stream);
-  if (c->verbose) std::printf("multi-RHS: K=%d cases, R=%d cases per thread, %d CTAs\n", M.K, M.R, M.grid_mv);
+  if (c->verbose) std::printf("multi-RHS: K=%d cases, C=%d cases per item, %d CTAs\n", M.K, M.C, M.grid_mv);
 }
 
 MultiState &multi_state(cfem_ctx *c, int K) {
@@ -148,7 +161,12 @@ MultiState &multi_state(cfem_ctx *c, int K) {
   M->grid_vec = (int)std::min<int64_t>(std::max<int64_t>(1, (int64_t)(((size_t)c->nn * K + kThreads - 1) / kThreads)),
                                        (int64_t)c->n_sm * 2);
   const int max_mv_grid = c->n_sm * 8;
-  M->partials.alloc((size_t)std::max(max_mv_grid, M->grid_vec) * K * 3);
+  const int max_grid = std::max(max_mv_grid, M->grid_vec);
+  M->partials.alloc((size_t)max_grid * K * 3);
+  const int max_groups = (max_grid + kSumGroup - 1) / kSumGroup;
+  M->gpart.alloc((size_t)max_groups * K * 3);
+  M->gcnt.alloc((size_t)2 * max_groups);
+  M->gcnt.zero(c->stream);
   return *M;
 }
 
@@ -168,6 +186,7 @@ void run_pcg_multi(cfem_ctx *c, MultiState &M, int k_active, double tol, int rul
   h.maxit = maxit > 0 ? maxit : 1000000;
   h.k_active = k_active;
   CK(cudaMemcpyAsync(M.ctl.p, &h, sizeof(MultiCtl), cudaMemcpyHostToDevice, c->stream));
+  M.gcnt.zero(c->stream);  // (tickets of a launch that stopped early are not left behind)
   MultiParams<float> P = multi_params(c, M);
   launch_vec(c, M, P, nullptr, 1);
   if (!M.graph) {
@@ -178,7 +197,7 @@ void run_pcg_multi(cfem_ctx *c, MultiState &M, int k_active, double tol, int rul
       for (int it = 0; it < c->chunk; ++it) {
         float *pold = (it & 1) ? M.pB.p : M.pA.p;
         float *pnew = (it & 1) ? M.pA.p : M.pB.p;
-        launch_mvm_r(c, M, MV_PCG, P, M.z.p, pold, pnew, M.u.p);
+        launch_mvm_c(c, M, MV_PCG, P, M.z.p, pold, pnew, M.u.p);
         launch_vec(c, M, P, pnew, 0);
       }
     } catch (...) {
@@ -239,10 +258,10 @@ cfem_status solve_batch(cfem_ctx *c, const cfem_solve_params &p, int kb, const d
   k_multi_to_internal<double><<<nblk(nitems), kThreads, 0, c->stream>>>(nn, K, kb, c->nd, M.io.p,
                                                                          c->node_new2old.p, M.f64.p);
   CKL();
-  if (!M.R) {
+  if (!M.C) {
     k_convert<double, float><<<nblk(nitems * 4), kThreads, 0, c->stream>>>(nitems * 4, M.f64.p, M.f.p);
     CKL();
-    autotune_r(c, M);
+    autotune_c(c, M);
   }
   CK(cudaEventRecord(c->ev0, c->stream));
   std::vector<int> iters(kb, 0), outer(kb, 0), status(kb, CFEM_ERR_NOT_CONVERGED);

@@ -51,15 +51,16 @@ __host__ __device__ __forceinline__ int half_slot_count(int h, int len) {
 // a lane shuffle with half 1 (combine_half_forces)
 __host__ __device__ __forceinline__ bool half_writes(int h, int hs) { return h == 0 || hs >= 3; }
 
-// Adds half 1's P, Q and R_3 forces to half 0's (lanes 2f and 2f + 1); every
-// lane of the warp takes part.
-template <typename T, int DIM>
+// Adds half 1's P, Q and R_3 forces to half 0's (lanes l and l ^ X: X = 1 for
+// one case per lane pair, X = C when the lanes of a half-fan carry C cases);
+// every lane of the warp takes part.
+template <typename T, int DIM, int X = 1>
 __device__ __forceinline__ void combine_half_forces(T (&fv)[6][DIM], int h) {
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
-    const T p = __shfl_xor_sync(0xffffffffu, fv[0][d], 1);
-    const T q = __shfl_xor_sync(0xffffffffu, fv[1][d], 1);
-    const T r = __shfl_xor_sync(0xffffffffu, h ? fv[2][d] : fv[5][d], 1);
+    const T p = __shfl_xor_sync(0xffffffffu, fv[0][d], X);
+    const T q = __shfl_xor_sync(0xffffffffu, fv[1][d], X);
+    const T r = __shfl_xor_sync(0xffffffffu, h ? fv[2][d] : fv[5][d], X);
     if (h == 0) {
       fv[0][d] += p;
       fv[1][d] += q;

@@ -1,12 +1,14 @@
 // Multi-right-hand-side EbE PCG: k load cases on one mesh (3D, edge-fan form).
 //
 // Node vectors hold all K cases of a node contiguously: [node][K][4] (K >= k,
-// a power of two <= kMaxCases; unused cases stay zero). The matvec loads each
-// patch block (kernels_fan_tma.cuh) once and applies it to the K cases in
-// passes of R: every half-fan thread evaluates its tets for R cases at once,
-// so each gradient read from shared memory serves R cases. Every case has its
-// own PCG scalars and stopping test; a converged case is frozen (its passes
-// are skipped once all R cases of a pass are done).
+// a power of two <= kMaxCases; unused cases stay zero). The matvec works on
+// items (patch, chunk of C cases): the lanes of a warp hold C cases of 32 / C
+// half-fans, so a node's values for the chunk are one contiguous C x 16-byte
+// load, every gradient read from the patch block (kernels_fan_tma.cuh) is a
+// broadcast serving C cases, and the forces are summed per node and case in
+// shared memory by atomics whose lanes never share an address. Every case has
+// its own PCG scalars and stopping test; a converged case is frozen (its items
+// are skipped once all C cases of a chunk are done).
 #pragma once
 
 #include "kernels.cuh"
@@ -15,6 +17,7 @@
 namespace cfem {
 
 constexpr int kMaxCases = 256;
+constexpr int kSumGroup = 16;  // blocks per group of the first level of the per-case grid sums
 
 struct MultiScalars {  // per case
   double gamma, gamma_prev, gamma0, sigma, alpha, beta, rr, ff;
@@ -39,287 +42,318 @@ struct MultiParams {
   MultiScalars *sc;     // [K]
   MultiCtl *ctl;
   double *partials;     // [grid][K] (matvec) / [grid][K][3] (vector kernels)
+  double *gpart;        // [grid / kSumGroup][K][3] group sums of the partials
+  unsigned *gcnt_mv, *gcnt_up;  // [grid / kSumGroup] group tickets of the matvec / vector kernel
   FanTmaParams F;       // patch blocks (layout and fan offsets)
 };
 
-// Shared memory of k_matvec_multi: one patch block, R force lists, R staged node blocks.
-inline size_t multi_smem_bytes(const FanBlockLayout &L, int R) {
-  const int fs_bytes = kFanForces * kFanThreads * 4 * (int)sizeof(float);
-  return (size_t)L.bytes + (size_t)R * fs_bytes + (size_t)R * L.npn * 4 * sizeof(float) + 16 +
-         (size_t)kMaxCases * sizeof(double) + 64;
+// Shared memory of k_matvec_multi<MODE, C> for K cases: the patch block, the
+// staged node values [npn][C][4], per-case energies [K] and warp partials
+// [8][C] (double), the mbarrier, the force sums [npn][3][C], per-case beta and
+// done flags [K].
+struct MultiSmem {
+  int sp, en, red, bar, sy, beta, done, bytes;
+};
+__host__ __device__ inline MultiSmem multi_smem(const FanBlockLayout &L, int C, int K) {
+  MultiSmem m{};
+  int off = L.bytes;
+  m.sp = off; off += L.npn * C * 16;
+  m.en = off; off += K * 8;
+  m.red = off; off += (kHfanThreads / 32) * C * 8;
+  m.bar = off; off += 16;
+  m.sy = off; off += L.npn * 3 * C * 4;
+  m.beta = off; off += K * 4;
+  m.done = off; off += K * 4;
+  m.bytes = off;
+  return m;
 }
 
-// Last-block helper: per case c < K the sums over the grid's blocks b of
-// partials[(b * K + c) * NQ + k], in a fixed order, into out[c * NQ + k].
-// Many cases: one thread per case with eight interleaved partial sums, so that
-// its loads overlap. Few cases: one warp per case, four interleaved partial
-// sums per lane and a shuffle tree. Called by all threads of the last block.
+// Per-case grid sums in two fixed-order levels. Every block calls it (all
+// threads) once its partials part[(b * K + c) * NQ + k] are written. The last
+// block of each group of kSumGroup blocks adds the group's partials in block
+// order into gpart[(g * K + c) * NQ + k]; the last of those group finishers
+// adds the groups in group order into out[c * NQ + k] (shared memory) and
+// returns true there, false everywhere else (uniform per block). Each level
+// is one round of independent loads per sum instead of a chain over all blocks.
+// The tickets return to zero for the next launch.
 template <int NQ>
-__device__ __forceinline__ void case_sums(const double *partials, int nblocks, int K, double *out) {
-  if (K >= 128) {
-    for (int c = threadIdx.x; c < K; c += blockDim.x) {
+__device__ __forceinline__ bool tree_case_sums(const double *part, double *gpart, unsigned *gcnt, unsigned *top, int K,
+                                               double *out) {
+  __shared__ bool s_last;
+  const int n = K * NQ;
+  const int g = blockIdx.x / kSumGroup, ng = (gridDim.x + kSumGroup - 1) / kSumGroup;
+  const int b0 = g * kSumGroup, nb = min(kSumGroup, (int)gridDim.x - b0);
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(&gcnt[g], 1u) == (unsigned)(nb - 1);
+  __syncthreads();
+  if (!s_last) return false;
+  __threadfence();
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    double v[kSumGroup];
 #pragma unroll
-      for (int k = 0; k < NQ; ++k) {
-        double s8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        int b = 0;
-        for (; b + 8 <= nblocks; b += 8)
+    for (int q = 0; q < kSumGroup; ++q) v[q] = q < nb ? __ldcg(part + (size_t)(b0 + q) * n + j) : 0.0;
+    double t = 0;
 #pragma unroll
-          for (int q = 0; q < 8; ++q) s8[q] += __ldcg(partials + ((size_t)(b + q) * K + c) * NQ + k);
-#pragma unroll
-        for (int q = 0; q < 7; ++q)
-          if (b + q < nblocks) s8[q] += __ldcg(partials + ((size_t)(b + q) * K + c) * NQ + k);
-        out[c * NQ + k] = ((s8[0] + s8[1]) + (s8[2] + s8[3])) + ((s8[4] + s8[5]) + (s8[6] + s8[7]));
-      }
-    }
-    return;
+    for (int q = 0; q < kSumGroup; ++q) t += v[q];
+    gpart[(size_t)g * n + j] = t;
   }
-  const int lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
-  for (int c = threadIdx.x >> 5; c < K; c += nwarp) {
+  if (threadIdx.x == 0) gcnt[g] = 0;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(top, 1u) == (unsigned)(ng - 1);
+  __syncthreads();
+  if (!s_last) return false;
+  __threadfence();
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    double t = 0;
+    for (int g0 = 0; g0 < ng; g0 += kSumGroup) {
+      double v[kSumGroup];
 #pragma unroll
-    for (int k = 0; k < NQ; ++k) {
-      double s4[4] = {0, 0, 0, 0};
-      int b = lane;
-      for (; b + 96 < nblocks; b += 128)
+      for (int q = 0; q < kSumGroup; ++q) v[q] = g0 + q < ng ? __ldcg(gpart + (size_t)(g0 + q) * n + j) : 0.0;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) s4[q] += __ldcg(partials + ((size_t)(b + 32 * q) * K + c) * NQ + k);
-#pragma unroll
-      for (int q = 0; q < 3; ++q)
-        if (b + 32 * q < nblocks) s4[q] += __ldcg(partials + ((size_t)(b + 32 * q) * K + c) * NQ + k);
-      double t = (s4[0] + s4[1]) + (s4[2] + s4[3]);
-      for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
-      if (lane == 0) out[c * NQ + k] = t;
+      for (int q = 0; q < kSumGroup; ++q) t += v[q];
     }
+    out[j] = t;
   }
+  if (threadIdx.x == 0) *top = 0;
+  __syncthreads();
+  return true;
 }
 
 // y_c += K' p_c for the K cases. PCG (MODE MV_PCG): p_c = z_c + beta_c p_old_c
 // staged on the fly (written back by the owning patch), sigma_c = p_c.K'p_c.
 // PLAIN: y_c += K' x_c. FP32 only (the patch blocks hold FP32 gradients).
-template <int MODE, int R>
-__global__ void __launch_bounds__(kHfanThreads) k_matvec_multi(MultiParams<float> P, const float *x, const float *pold,
-                                                               float *pnew, float *y) {
+//
+// Items q = patch * (K / C) + chunk; CTA b takes the contiguous items
+// [n b / G, n (b + 1) / G), so the chunks of a patch reuse its block. Lane l of
+// warp w holds case l % C of half-fan (round * 8 + w) * (32 / C) + l / C: the
+// two halves of a fan are lanes l and l ^ C. A thread's case (l % C) is the
+// same in every phase, so its energy partial needs no exchange until the end
+// of the item.
+template <int MODE, int C>
+__global__ void __launch_bounds__(kHfanThreads, 2) k_matvec_multi(MultiParams<float> P, const float *x,
+                                                                  const float *pold, float *pnew, float *y) {
   using T = float;
-  constexpr int DIM = 3, VW = 4;
+  constexpr int DIM = 3, VW = 4, NW = kHfanThreads / 32;
+  constexpr int HPW = 32 / C;                    // half-fans per warp and round
+  constexpr int ROUNDS = kHfanThreads / (NW * HPW);
+  constexpr int SU = 4;                          // staging items in flight per thread
+  static_assert(C >= 2 && C <= 16 && (C & (C - 1)) == 0, "C: 2, 4, 8 or 16 cases per item");
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const FanBlockLayout &L = P.F.L;
-  const int K = P.K;
+  const int K = P.K, NC = K / C;
+  const MultiSmem S = multi_smem(L, C, K);
   unsigned char *B = smem_raw;
-  // case-fastest layouts: the R cases of one node (or force slot) are adjacent
-  T *fs = reinterpret_cast<T *>(smem_raw + L.bytes);                            // [kFanForces * kFanThreads][R][4]
-  constexpr int FS = kFanForces * kFanThreads * VW;
-  T *sp = fs + (size_t)R * FS;                                                  // [npn][R][4]
-  uint64_t *bar = reinterpret_cast<uint64_t *>(sp + (size_t)R * L.npn * VW);
-  double *s_en = reinterpret_cast<double *>(bar + 2);                           // [K] energies of this block
+  T *sp = reinterpret_cast<T *>(smem_raw + S.sp);
+  double *s_en = reinterpret_cast<double *>(smem_raw + S.en);
+  double *s_red = reinterpret_cast<double *>(smem_raw + S.red);
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw + S.bar);
+  T *sy = reinterpret_cast<T *>(smem_raw + S.sy);
+  T *s_beta = reinterpret_cast<T *>(smem_raw + S.beta);
+  int *s_done = reinterpret_cast<int *>(smem_raw + S.done);
   if (MODE == MV_PCG && P.ctl->all_done) return;
-  for (int c = threadIdx.x; c < K; c += blockDim.x) s_en[c] = 0;
+  for (int c = threadIdx.x; c < K; c += blockDim.x) {
+    s_en[c] = 0;
+    s_done[c] = 0;
+    s_beta[c] = 0;
+    if (MODE == MV_PCG) {
+      const MultiScalars &sc = P.sc[c];
+      s_done[c] = sc.done;
+      s_beta[c] = sc.done ? T(0) : (T)sc.beta;
+    }
+  }
+  for (int i = threadIdx.x; i < L.npn * 3 * C; i += blockDim.x) sy[i] = 0;
   if (threadIdx.x == 0) {
     mbar_init(&bar[0], 1);
     fence_mbar_init();
   }
   __syncthreads();
-  const uint16_t *fstart = reinterpret_cast<const uint16_t *>(B + L.fstart_off);
   const int32_t *nodes = reinterpret_cast<const int32_t *>(B + L.nodes_off);
   const uint8_t *bits = B + L.bits_off;
-  int it = 0;
-  for (int patch = blockIdx.x; patch < P.n_patches; patch += gridDim.x, ++it) {
-    fence_proxy_async();  // earlier reads of the block precede the copy that overwrites it
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      mbar_expect_tx(&bar[0], (unsigned)L.bytes);
-      bulk_load(B, P.F.blocks + (size_t)patch * L.bytes, (unsigned)L.bytes, &bar[0]);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int cl = lane & (C - 1), hs = lane / C, h = hs & 1;
+  const T lam = P.lam, mu = P.mu;
+  const int64_t n_items = (int64_t)P.n_patches * NC;
+  const int64_t q0 = n_items * blockIdx.x / gridDim.x, q1 = n_items * (blockIdx.x + 1) / gridDim.x;
+  int cur = -1;
+  unsigned nload = 0;
+  for (int64_t q = q0; q < q1; ++q) {
+    const int patch = (int)(q / NC), c0 = (int)(q - (int64_t)patch * NC) * C;
+    if (MODE == MV_PCG) {
+      bool all = true;  // (uniform: read from shared memory)
+#pragma unroll
+      for (int r = 0; r < C; ++r) all &= s_done[c0 + r] != 0;
+      if (all) continue;
     }
-    const bool ok = mbar_wait_bounded(&bar[0], (unsigned)(it & 1));
-    if (__syncthreads_or(!ok)) {
-      if (threadIdx.x == 0) atomicOr(P.F.err, kErrTmaTimeout);
-      return;
+    if (patch != cur) {
+      fence_proxy_async();  // earlier reads of the block precede the copy that overwrites it
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        mbar_expect_tx(&bar[0], (unsigned)L.bytes);
+        bulk_load(B, P.F.blocks + (size_t)patch * L.bytes, (unsigned)L.bytes, &bar[0]);
+      }
+      const bool ok = mbar_wait_bounded(&bar[0], nload & 1u);
+      ++nload;
+      if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) atomicOr(P.F.err, kErrTmaTimeout);
+        return;
+      }
+      cur = patch;
     }
     const int32_t *hdr = reinterpret_cast<const int32_t *>(B + L.hdr_off);
     const int nn = hdr[0], own = hdr[1];
-    const int h = threadIdx.x & 1;
-    int slot[6];
-    const int nk = load_half_slots(B + L.slot_off, threadIdx.x, slot);
-    for (int c0 = 0; c0 < K; c0 += R) {
-      if (MODE == MV_PCG) {
-        // every thread evaluates the pass's cases itself; the barrier's AND
-        // makes the decision uniform without a shared flag
-        int all = 1;
+    const int n_it = nn * C;  // staging / output items (node i, case cl): it = i * C + cl
+    const T beta = MODE == MV_PCG ? s_beta[c0 + cl] : T(0);
+    // 1. stage the chunk's node values: C cases of a node are one contiguous load
+    for (int i0 = threadIdx.x; i0 < n_it; i0 += SU * kHfanThreads) {
+      NodeV<T, VW> v[SU], w[SU];
+      int gi[SU];
 #pragma unroll
-        for (int r = 0; r < R; ++r) all &= P.sc[c0 + r].done != 0;
-        if (__syncthreads_and(all)) continue;
+      for (int u = 0; u < SU; ++u) {
+        const int it = i0 + u * kHfanThreads;
+        gi[u] = it < n_it ? nodes[it / C] : -1;
+        if (gi[u] >= 0) {
+          const int64_t idx = (int64_t)gi[u] * K + c0 + cl;
+          v[u] = ldv<T, VW>(x, idx);
+          if (MODE == MV_PCG && beta != T(0)) w[u] = ldv<T, VW>(pold, idx);
+        }
       }
-      // 1. stage: items (node i, case r), case fastest
-      for (int q = threadIdx.x; q < nn * R; q += kHfanThreads) {
-        const int i = q / R, r = q - i * R, c = c0 + r;
-        const int g = nodes[i];
-        const int64_t idx = (int64_t)g * K + c;
-        NodeV<T, VW> v = ldv<T, VW>(x, idx);
-        if (MODE == MV_PCG) {
-          const MultiScalars &s = P.sc[c];
-          if (!s.done && s.beta != 0.0) {
-            const T beta = (T)s.beta;
-            const NodeV<T, VW> po = ldv<T, VW>(pold, idx);
 #pragma unroll
-            for (int d = 0; d < DIM; ++d) v.v[d] += beta * po.v[d];
+      for (int u = 0; u < SU; ++u) {
+        if (gi[u] < 0) continue;
+        const int it = i0 + u * kHfanThreads, i = it / C;
+        if (MODE == MV_PCG) {
+          if (beta != T(0)) {
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) v[u].v[d] += beta * w[u].v[d];
           }
-          if (i >= own) stv<T, VW>(pnew, idx, v);
+          if (i >= own) stv<T, VW>(pnew, (int64_t)gi[u] * K + c0 + cl, v[u]);
         }
         const unsigned bb = bits[i];
         NodeV<T, VW> m;
 #pragma unroll
-        for (int d = 0; d < VW; ++d) m.v[d] = (d < DIM && !(bb >> d & 1u)) ? v.v[d] : T(0);
-        stv<T, VW>(sp, (int64_t)i * R + r, m);
+        for (int d = 0; d < VW; ++d) m.v[d] = (d < DIM && !(bb >> d & 1u)) ? v[u].v[d] : T(0);
+        stv<T, VW>(sp, it, m);
       }
-      __syncthreads();
-      // 2. half-fans, R cases per thread
-      T fv[R][6][DIM];
-      T e_fan[R];
-      {
-        T uv[R][6][DIM];
+    }
+    __syncthreads();
+    // 2. half-fans: forces relative to P (missing tets have zero gradients),
+    //    halves combined by shuffle, sums by shared atomics per (node, case)
+    Comp32 energy;
+#pragma unroll 1
+    for (int rd = 0; rd < ROUNDS; ++rd) {
+      const int hf = (rd * NW + wid) * HPW + hs;
+      int slot[6];
+      const int nk = load_half_slots(B + L.slot_off, hf, slot);
+      T du[6][DIM], fv[6][DIM];
 #pragma unroll
-        for (int k = 0; k < 6; ++k) {
-          const int li = k < nk ? slot[k] : 0;
+      for (int k = 0; k < 6; ++k) {
+        NodeV<T, VW> s;
 #pragma unroll
-          for (int r = 0; r < R; ++r) {
-            NodeV<T, VW> s;
+        for (int d = 0; d < VW; ++d) s.v[d] = 0;
+        if (k < nk) s = ldv<T, VW>(sp, slot[k] * C + cl);
 #pragma unroll
-            for (int d = 0; d < VW; ++d) s.v[d] = 0;
-            if (k < nk) s = ldv<T, VW>(sp, (int64_t)li * R + r);
-#pragma unroll
-            for (int d = 0; d < DIM; ++d) {
-              uv[r][k][d] = s.v[d];
-              fv[r][k][d] = 0;
-            }
-          }
-        }
-#pragma unroll
-        for (int r = 0; r < R; ++r) e_fan[r] = 0;
-#pragma unroll
-        for (int jj = 0; jj < 3; ++jj) {
-          if (jj + 3 < nk) {
-            T G[9];
-            load_tet_G(B + L.g_off, threadIdx.x, jj, G);
-#pragma unroll
-            for (int r = 0; r < R; ++r) {
-              T u[4][DIM], fe[4][DIM];
-#pragma unroll
-              for (int d = 0; d < DIM; ++d) {
-                u[0][d] = uv[r][0][d];
-                u[1][d] = uv[r][1][d];
-                u[2][d] = uv[r][2 + jj][d];
-                u[3][d] = uv[r][3 + jj][d];
-              }
-              element_force<T, DIM>(u, G, P.lam, P.mu, T(1), T(0), fe);
-#pragma unroll
-              for (int d = 0; d < DIM; ++d) {
-                if (MODE == MV_PCG)
-                  e_fan[r] += u[0][d] * fe[0][d] + u[1][d] * fe[1][d] + u[2][d] * fe[2][d] + u[3][d] * fe[3][d];
-                fv[r][0][d] += fe[0][d];
-                fv[r][1][d] += fe[1][d];
-                fv[r][2 + jj][d] += fe[2][d];
-                fv[r][3 + jj][d] += fe[3][d];
-              }
-            }
-          }
+        for (int d = 0; d < DIM; ++d) {
+          du[k][d] = s.v[d];
+          fv[k][d] = 0;
         }
       }
 #pragma unroll
-      for (int r = 0; r < R; ++r) combine_half_forces<T, DIM>(fv[r], h);
+      for (int k = 1; k < 6; ++k)
 #pragma unroll
-      for (int r = 0; r < R; ++r)
+        for (int d = 0; d < DIM; ++d) du[k][d] -= du[0][d];
 #pragma unroll
-        for (int k = 0; k < 6; ++k)
-          if (k < nk && half_writes(h, k)) {
-            NodeV<T, VW> o;
+      for (int jj = 0; jj < 3; ++jj) {
+        T G[9];
+        load_tet_G(B + L.g_off, hf, jj, G);
+        T f1[3], f2[3], f3[3];
+        tet_forces_rel<T>(du[1], du[2 + jj], du[3 + jj], G, lam, mu, f1, f2, f3);
 #pragma unroll
-            for (int d = 0; d < VW; ++d) o.v[d] = d < DIM ? fv[r][k][d] : T(0);
-            stv<T, VW>(fs, (int64_t)half_fpos(B + L.fpos_off, threadIdx.x, k) * R + r, o);
-          }
-      __syncthreads();
-      // 3. node sums: items (node i, case r)
-      DotAcc<T> e_diag[R];
-      for (int q = threadIdx.x; q < nn * R; q += kHfanThreads) {
-        const int i = q / R, r = q - i * R, c = c0 + r;
-        const int g = nodes[i];
-        const unsigned bb = bits[i];
-        T acc[DIM] = {0, 0, 0};
-        const int k1 = fstart[i + 1];
-        for (int k = fstart[i]; k < k1; ++k) {
-          const NodeV<T, VW> fo = ldv<T, VW>(fs, (int64_t)k * R + r);
-#pragma unroll
-          for (int d = 0; d < DIM; ++d) acc[d] += fo.v[d];
-        }
-        NodeV<T, VW> out;
-        bool any = false;
-#pragma unroll
-        for (int d = 0; d < VW; ++d) {
-          T val = (d < DIM && !(bb >> d & 1u)) ? acc[d < DIM ? d : 0] : T(0);
-          out.v[d] = val;
-          any |= val != T(0);
-        }
-        const int64_t idx = (int64_t)g * K + c;
-        if (bb && i >= own) {
-          NodeV<T, VW> v = ldv<T, VW>(MODE == MV_PCG ? pnew : x, idx);  // this block wrote pnew[idx] while staging
-          NodeV<T, VW> dg = ldv<T, VW>(P.diagA, g);
-#pragma unroll
-          for (int d = 0; d < DIM; ++d)
-            if (bb >> d & 1u) {
-              T t = dg.v[d] * v.v[d];
-              out.v[d] = t;
-              any |= t != T(0);
-              if (MODE == MV_PCG) {
-#pragma unroll
-                for (int rr = 0; rr < R; ++rr)
-                  if (rr == r) e_diag[rr].add(t * v.v[d]);
-              }
-            }
-        }
-        if (any) atomic_addv<T, VW>(y, idx, out, DIM);
-      }
-      // per-case energies of this pass, summed over the block in a fixed order
-      if (MODE == MV_PCG) {
-        __shared__ double s_red[R][kHfanThreads / 32];
-        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-          Comp32 cm;
-          cm.add(e_fan[r]);
-          cm.merge(e_diag[r].c.hi, e_diag[r].c.lo);
-          for (int o = 16; o > 0; o >>= 1) {
-            const float h2 = __shfl_down_sync(0xffffffffu, cm.hi, o), l2 = __shfl_down_sync(0xffffffffu, cm.lo, o);
-            cm.merge(h2, l2);
-          }
-          if (lane == 0) s_red[r][wid] = (double)cm.hi + (double)cm.lo;
-        }
-        __syncthreads();
-        if (threadIdx.x < R) {
-          double t = 0;
-          for (int w = 0; w < kHfanThreads / 32; ++w) t += s_red[threadIdx.x][w];
-          s_en[c0 + threadIdx.x] += t;
+        for (int d = 0; d < DIM; ++d) {
+          fv[1][d] += f1[d];
+          fv[2 + jj][d] += f2[d];
+          fv[3 + jj][d] += f3[d];
         }
       }
-      __syncthreads();  // sp / fs of this pass are free again
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) fv[0][d] = -(fv[1][d] + fv[2][d] + fv[3][d] + fv[4][d] + fv[5][d]);
+      if (MODE == MV_PCG) {  // the forces sum to zero: sum_k u_k.f_k = sum_k>0 du_k.f_k
+        T e = 0;
+#pragma unroll
+        for (int k = 1; k < 6; ++k)
+#pragma unroll
+          for (int d = 0; d < DIM; ++d) e += du[k][d] * fv[k][d];
+        energy.add(e);
+      }
+      combine_half_forces<T, DIM, C>(fv, h);
+#pragma unroll
+      for (int k = 0; k < 6; ++k)
+        if (k < nk && half_writes(h, k)) {
+#pragma unroll
+          for (int d = 0; d < DIM; ++d) atomicAdd(sy + (slot[k] * 3 + d) * C + cl, fv[k][d]);
+        }
+    }
+    __syncthreads();
+    // 3. node sums out (and cleared), constrained DOFs: (I - P) diag(A) p on owned nodes
+    for (int it = threadIdx.x; it < n_it; it += kHfanThreads) {
+      const int i = it / C;
+      const unsigned bb = bits[i];
+      NodeV<T, VW> out;
+      bool any = false;
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) {
+        T *a = sy + (i * 3 + d) * C + cl;
+        out.v[d] = (bb >> d & 1u) ? T(0) : *a;
+        *a = 0;
+        any |= out.v[d] != T(0);
+      }
+      out.v[3] = 0;
+      const int g = nodes[i];
+      const int64_t idx = (int64_t)g * K + c0 + cl;
+      if (bb && i >= own) {
+        const NodeV<T, VW> v = ldv<T, VW>(MODE == MV_PCG ? pnew : x, idx);  // this block wrote pnew[idx] while staging
+        const NodeV<T, VW> dg = ldv<T, VW>(P.diagA, g);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d)
+          if (bb >> d & 1u) {
+            const T t = dg.v[d] * v.v[d];
+            out.v[d] = t;
+            any |= t != T(0);
+            if (MODE == MV_PCG) energy.add(t * v.v[d]);
+          }
+      }
+      if (any) atomic_addv<T, VW>(y, idx, out, DIM);
+    }
+    if (MODE == MV_PCG) {  // per-case energy of the item: lanes of one case, then warps in order
+#pragma unroll
+      for (int o = C; o < 32; o <<= 1) {
+        const float h2 = __shfl_xor_sync(0xffffffffu, energy.hi, o), l2 = __shfl_xor_sync(0xffffffffu, energy.lo, o);
+        energy.merge(h2, l2);
+      }
+      if (lane < C) s_red[wid * C + lane] = (double)energy.hi + (double)energy.lo;
+    }
+    __syncthreads();  // sp, sy and s_red of this item are complete
+    if (MODE == MV_PCG && threadIdx.x < C) {
+      double t = 0;
+#pragma unroll
+      for (int w = 0; w < NW; ++w) t += s_red[w * C + threadIdx.x];
+      s_en[c0 + threadIdx.x] += t;
     }
   }
   if (MODE != MV_PCG) return;
-  // per-case grid sums: the last block adds the block partials in block order
+  // per-case grid sums (fixed-order tree), alpha_c = gamma_c / sigma_c in the last block
+  __syncthreads();
   for (int c = threadIdx.x; c < K; c += blockDim.x) P.partials[(size_t)blockIdx.x * K + c] = s_en[c];
-  __shared__ bool last;
-  __threadfence();
   __syncthreads();
-  if (threadIdx.x == 0) last = atomicAdd(&P.ctl->count_mv, 1u) == gridDim.x - 1;
-  __syncthreads();
-  if (!last) return;
-  __threadfence();
-  __shared__ double s_tot[kMaxCases];
-  case_sums<1>(P.partials, gridDim.x, K, s_tot);
-  __syncthreads();
+  double *s_tot = s_en;  // (the block's own energies are in the partials now)
+  if (!tree_case_sums<1>(P.partials, P.gpart, P.gcnt_mv, &P.ctl->count_mv, K, s_tot)) return;
   for (int c = threadIdx.x; c < K; c += blockDim.x) {
     const double t = s_tot[c];
     MultiScalars &s = P.sc[c];
     s.sigma = t;
     s.alpha = s.done ? 0.0 : s.gamma / t;
   }
-  if (threadIdx.x == 0) P.ctl->count_mv = 0;
 }
 
 // Per case: init (r = f, x = 0) or update (x += alpha p, r -= alpha u),
@@ -411,18 +445,11 @@ __global__ void __launch_bounds__(kThreads) k_pcg_multi_vec(MultiParams<T> P, T 
     double *pt = P.partials + ((size_t)blockIdx.x * K + cc) * 3;
     pt[0] = a; pt[1] = b; pt[2] = e;
   }
-  __shared__ bool last;
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) last = atomicAdd(&P.ctl->count_up, 1u) == gridDim.x - 1;
-  __syncthreads();
-  if (!last) return;
-  __threadfence();
+  __syncthreads();  // (red is reused for the totals)
+  double *s_tot = &red[0][0];  // [K][3] (K <= kThreads)
+  if (!tree_case_sums<3>(P.partials, P.gpart, P.gcnt_up, &P.ctl->count_up, K, s_tot)) return;
   __shared__ int s_active;
   if (threadIdx.x == 0) s_active = 0;
-  __syncthreads();
-  double *s_tot = &red[0][0];  // [K][3] (K <= kThreads)
-  case_sums<3>(P.partials, gridDim.x, K, s_tot);
   __syncthreads();
   for (int cc = threadIdx.x; cc < K; cc += blockDim.x) {
     const double a = s_tot[cc * 3], b = s_tot[cc * 3 + 1], e = s_tot[cc * 3 + 2];
@@ -454,7 +481,6 @@ __global__ void __launch_bounds__(kThreads) k_pcg_multi_vec(MultiParams<T> P, T 
   if (threadIdx.x == 0) {
     if (!init) P.ctl->iter += 1;
     P.ctl->all_done = s_active == 0;
-    P.ctl->count_up = 0;
   }
 }
 
