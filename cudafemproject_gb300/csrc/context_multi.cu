@@ -7,6 +7,7 @@
 // formed case by case with the FP64 operator. Other forms and FP64 solve the
 // cases one after the other.
 #include <chrono>
+#include <cstdlib>
 
 #include "context_internal.cuh"
 #include "kernels_aux.cuh"
@@ -53,8 +54,7 @@ void launch_mvm_c(cfem_ctx *c, MultiState &M, int mode, const MultiParams<float>
                   const float *pold, float *pnew, float *y) {
   if (M.C == 2) launch_mvm<2>(c, M, mode, P, x, pold, pnew, y);
   else if (M.C == 4) launch_mvm<4>(c, M, mode, P, x, pold, pnew, y);
-  else if (M.C == 8) launch_mvm<8>(c, M, mode, P, x, pold, pnew, y);
-  else launch_mvm<16>(c, M, mode, P, x, pold, pnew, y);
+  else launch_mvm<8>(c, M, mode, P, x, pold, pnew, y);
 }
 
 template <int C>
@@ -62,8 +62,7 @@ const void *mvm_kernel_c(int mode) {
   return mode == MV_PCG ? (const void *)k_matvec_multi<MV_PCG, C> : (const void *)k_matvec_multi<MV_PLAIN, C>;
 }
 const void *mvm_kernel(int C, int mode) {
-  return C == 2 ? mvm_kernel_c<2>(mode) : C == 4 ? mvm_kernel_c<4>(mode) : C == 8 ? mvm_kernel_c<8>(mode)
-                                                                                  : mvm_kernel_c<16>(mode);
+  return C == 2 ? mvm_kernel_c<2>(mode) : C == 4 ? mvm_kernel_c<4>(mode) : mvm_kernel_c<8>(mode);
 }
 
 MultiParams<float> multi_params(cfem_ctx *c, MultiState &M) {
@@ -113,22 +112,29 @@ bool configure_c(cfem_ctx *c, MultiState &M, int C) {
 }
 
 // Cases per item: the variant with the shortest matvec on this mesh and
-// batch size, timed on the context's stream (PLAIN form, current vectors).
+// batch size, timed on the context's stream (PLAIN form, current vectors; the
+// best of three runs of four launches each). CFEM_MULTI_CASES=2|4|8 fixes it
+// (when that width fits in shared memory).
 void autotune_c(cfem_ctx *c, MultiState &M) {
   float best = 1e30f;
-  int best_c = 0;
-  for (int C : {2, 4, 8, 16}) {
+  int best_c = 0, forced = 0;
+  if (const char *e = std::getenv("CFEM_MULTI_CASES")) forced = std::atoi(e);
+  if ((forced != 2 && forced != 4 && forced != 8) || forced > M.K || !configure_c(c, M, forced)) forced = 0;
+  for (int C : {2, 4, 8}) {
     if (C > M.K) break;
+    if (forced && C != forced) continue;
     if (!configure_c(c, M, C)) continue;
     MultiParams<float> P = multi_params(c, M);
     launch_mvm_c(c, M, MV_PLAIN, P, M.f.p, nullptr, nullptr, M.u.p);  // warm-up
-    CK(cudaEventRecord(c->ev0, c->stream));
-    for (int i = 0; i < 3; ++i) launch_mvm_c(c, M, MV_PLAIN, P, M.f.p, nullptr, nullptr, M.u.p);
-    CK(cudaEventRecord(c->ev1, c->stream));
-    CK(cudaEventSynchronize(c->ev1));
-    float ms = 0;
-    CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
-    if (ms < best) { best = ms; best_c = C; }
+    for (int rep = 0; rep < 3; ++rep) {
+      CK(cudaEventRecord(c->ev0, c->stream));
+      for (int i = 0; i < 4; ++i) launch_mvm_c(c, M, MV_PLAIN, P, M.f.p, nullptr, nullptr, M.u.p);
+      CK(cudaEventRecord(c->ev1, c->stream));
+      CK(cudaEventSynchronize(c->ev1));
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+      if (ms < best) { best = ms; best_c = C; }
+    }
   }
   if (!best_c) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "multi-RHS patch too large for shared memory"};
   configure_c(c, M, best_c);

@@ -5,8 +5,8 @@
 // items (patch, chunk of C cases): the lanes of a warp hold C cases of 32 / C
 // half-fans, so a node's values for the chunk are one contiguous C x 16-byte
 // load, every gradient read from the patch block (kernels_fan_tma.cuh) is a
-// broadcast serving C cases, and the forces are summed per node and case in
-// shared memory by atomics whose lanes never share an address. Every case has
+// broadcast serving C cases, and the forces go to the block's node-sorted
+// force list ([entry][3][C]), whose runs the node sums add up without atomics. Every case has
 // its own PCG scalars and stopping test; a converged case is frozen (its items
 // are skipped once all C cases of a chunk are done).
 #pragma once
@@ -49,10 +49,10 @@ struct MultiParams {
 
 // Shared memory of k_matvec_multi<MODE, C> for K cases: the patch block, the
 // staged node values [npn][C][4], per-case energies [K] and warp partials
-// [8][C] (double), the mbarrier, the force sums [npn][3][C], per-case beta and
-// done flags [K].
+// [8][C] (double), the mbarrier, the force list [kFanForces x kFanThreads][3][C],
+// per-case beta and done flags [K].
 struct MultiSmem {
-  int sp, en, red, bar, sy, beta, done, bytes;
+  int sp, en, red, bar, fs, beta, done, bytes;
 };
 __host__ __device__ inline MultiSmem multi_smem(const FanBlockLayout &L, int C, int K) {
   MultiSmem m{};
@@ -61,7 +61,7 @@ __host__ __device__ inline MultiSmem multi_smem(const FanBlockLayout &L, int C, 
   m.en = off; off += K * 8;
   m.red = off; off += (kHfanThreads / 32) * C * 8;
   m.bar = off; off += 16;
-  m.sy = off; off += L.npn * 3 * C * 4;
+  m.fs = off; off += kFanForces * kFanThreads * 3 * C * 4;
   m.beta = off; off += K * 4;
   m.done = off; off += K * 4;
   m.bytes = off;
@@ -132,14 +132,14 @@ __device__ __forceinline__ bool tree_case_sums(const double *part, double *gpart
 // same in every phase, so its energy partial needs no exchange until the end
 // of the item.
 template <int MODE, int C>
-__global__ void __launch_bounds__(kHfanThreads, 2) k_matvec_multi(MultiParams<float> P, const float *x,
+__global__ void __launch_bounds__(kHfanThreads, C <= 2 ? 3 : 2) k_matvec_multi(MultiParams<float> P, const float *x,
                                                                   const float *pold, float *pnew, float *y) {
   using T = float;
   constexpr int DIM = 3, VW = 4, NW = kHfanThreads / 32;
   constexpr int HPW = 32 / C;                    // half-fans per warp and round
   constexpr int ROUNDS = kHfanThreads / (NW * HPW);
-  constexpr int SU = 4;                          // staging items in flight per thread
-  static_assert(C >= 2 && C <= 16 && (C & (C - 1)) == 0, "C: 2, 4, 8 or 16 cases per item");
+  constexpr int SU = C <= 2 ? 2 : 4;             // staging items in flight per thread
+  static_assert(C == 2 || C == 4 || C == 8, "C: 2, 4 or 8 cases per item");
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const FanBlockLayout &L = P.F.L;
   const int K = P.K, NC = K / C;
@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(kHfanThreads, 2) k_matvec_multi(MultiParams<fl
   double *s_en = reinterpret_cast<double *>(smem_raw + S.en);
   double *s_red = reinterpret_cast<double *>(smem_raw + S.red);
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw + S.bar);
-  T *sy = reinterpret_cast<T *>(smem_raw + S.sy);
+  T *fs = reinterpret_cast<T *>(smem_raw + S.fs);
   T *s_beta = reinterpret_cast<T *>(smem_raw + S.beta);
   int *s_done = reinterpret_cast<int *>(smem_raw + S.done);
   if (MODE == MV_PCG && P.ctl->all_done) return;
@@ -163,12 +163,12 @@ __global__ void __launch_bounds__(kHfanThreads, 2) k_matvec_multi(MultiParams<fl
       s_beta[c] = sc.done ? T(0) : (T)sc.beta;
     }
   }
-  for (int i = threadIdx.x; i < L.npn * 3 * C; i += blockDim.x) sy[i] = 0;
   if (threadIdx.x == 0) {
     mbar_init(&bar[0], 1);
     fence_mbar_init();
   }
   __syncthreads();
+  const uint16_t *fstart = reinterpret_cast<const uint16_t *>(B + L.fstart_off);
   const int32_t *nodes = reinterpret_cast<const int32_t *>(B + L.nodes_off);
   const uint8_t *bits = B + L.bits_off;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -239,7 +239,7 @@ __global__ void __launch_bounds__(kHfanThreads, 2) k_matvec_multi(MultiParams<fl
     }
     __syncthreads();
     // 2. half-fans: forces relative to P (missing tets have zero gradients),
-    //    halves combined by shuffle, sums by shared atomics per (node, case)
+    //    halves combined by shuffle, written to the force list
     Comp32 energy;
 #pragma unroll 1
     for (int rd = 0; rd < ROUNDS; ++rd) {
@@ -290,22 +290,28 @@ __global__ void __launch_bounds__(kHfanThreads, 2) k_matvec_multi(MultiParams<fl
 #pragma unroll
       for (int k = 0; k < 6; ++k)
         if (k < nk && half_writes(h, k)) {
+          T *o = fs + half_fpos(B + L.fpos_off, hf, k) * (3 * C) + cl;
 #pragma unroll
-          for (int d = 0; d < DIM; ++d) atomicAdd(sy + (slot[k] * 3 + d) * C + cl, fv[k][d]);
+          for (int d = 0; d < DIM; ++d) o[d * C] = fv[k][d];
         }
     }
     __syncthreads();
-    // 3. node sums out (and cleared), constrained DOFs: (I - P) diag(A) p on owned nodes
+    // 3. node sums over contiguous force runs, constrained DOFs: (I - P) diag(A) p on owned nodes
     for (int it = threadIdx.x; it < n_it; it += kHfanThreads) {
       const int i = it / C;
       const unsigned bb = bits[i];
+      T acc[DIM] = {0, 0, 0};
+      const int k1 = fstart[i + 1];
+      for (int k = fstart[i]; k < k1; ++k) {
+        const T *f = fs + k * (3 * C) + cl;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) acc[d] += f[d * C];
+      }
       NodeV<T, VW> out;
       bool any = false;
 #pragma unroll
       for (int d = 0; d < DIM; ++d) {
-        T *a = sy + (i * 3 + d) * C + cl;
-        out.v[d] = (bb >> d & 1u) ? T(0) : *a;
-        *a = 0;
+        out.v[d] = (bb >> d & 1u) ? T(0) : acc[d];
         any |= out.v[d] != T(0);
       }
       out.v[3] = 0;
@@ -333,7 +339,7 @@ __global__ void __launch_bounds__(kHfanThreads, 2) k_matvec_multi(MultiParams<fl
       }
       if (lane < C) s_red[wid * C + lane] = (double)energy.hi + (double)energy.lo;
     }
-    __syncthreads();  // sp, sy and s_red of this item are complete
+    __syncthreads();  // sp, fs and s_red of this item are complete
     if (MODE == MV_PCG && threadIdx.x < C) {
       double t = 0;
 #pragma unroll

@@ -172,3 +172,25 @@ def test_multi_rhs_many_cases():
         x, _ = o.pcg(F[i], tol=1e-14, rule=1)
         assert rel(U[i], x) <= 1e-8, i
         assert infos[i]["status"] == 0
+
+
+@pytest.mark.parametrize("cases_per_item", [2, 4, 8])
+def test_multi_rhs_each_item_width(cases_per_item, monkeypatch):
+    """The case-lane matvec at each chunk width (2, 4 or 8 cases per warp lane
+    group, fixed through CFEM_MULTI_CASES): 11 cases (padded to 16) match the
+    FP64 oracle, in FP32 + refinement and in plain FP32."""
+    from cudafemproject_gb300.solver import FemContext
+    monkeypatch.setenv("CFEM_MULTI_CASES", str(cases_per_item))
+    p = meshgen.box_3d(6, 6, 20, jitter=0.2, seed=9)
+    o = O.Oracle(p)
+    rng = np.random.default_rng(17 + cases_per_item)
+    F = rng.standard_normal((11, p.n_dof)) * 10.0 ** rng.uniform(2, 4, size=(11, 1))
+    ctx = FemContext(p)
+    U, infos = ctx.pcg_multi(F, precision="fp32_refine", tol=1e-4, stop_rule="residual", outer_tol=1e-12)
+    xs = {i: o.pcg(F[i], tol=1e-14, rule=1)[0] for i in (0, 5, 10)}
+    for i, x in xs.items():
+        assert rel(U[i], x) <= 1e-8, i
+        assert infos[i]["status"] == 0
+    U32, _ = ctx.pcg_multi(F, precision="fp32", tol=1e-6, stop_rule="residual")
+    for i, x in xs.items():
+        assert rel(U32[i], x) <= 1e-4, i
