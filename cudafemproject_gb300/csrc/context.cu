@@ -32,6 +32,8 @@ MvParams<T> base_mv_t(cfem_ctx *c) {
   P.cK = 1;
   P.cM = 0;
   P.partials = c->partials.p;
+  P.up_part = c->partials_up.p;
+  P.n_up = c->dim == 3 ? c->grid_upd : c->grid_vec;
   P.inc = c->inc.p;
   P.inc_start = c->inc_start.p;
   P.pe = c->prep.patch_elems;
@@ -105,6 +107,16 @@ void launch_mv_t(cfem_ctx *c, int mode, const MvParams<T> &P) {
   c->launches += 1;
 }
 
+// Grid of the PCG-form matvec that launch_mv_t runs for precision T (the
+// number of p.Ap partials the update kernel adds up).
+template <typename T>
+int pcg_mv_grid(const cfem_ctx *c) {
+  if constexpr (sizeof(T) == 4)
+    if (c->fans && c->fan_tma) return c->geo ? c->grid_geo : c->grid_ft32;
+  if (c->fans && c->dim == 3) return c->grid_fan;
+  return c->grid_mv;
+}
+
 template <typename T>
 VecParams<T> vec_params(cfem_ctx *c, Vecs<T> &V, T *p, Scalars *sc) {
   VecParams<T> P{};
@@ -114,6 +126,9 @@ VecParams<T> vec_params(cfem_ctx *c, Vecs<T> &V, T *p, Scalars *sc) {
   P.f = V.f.p;
   P.sc = sc;
   P.partials = c->partials.p;
+  P.mv_part = c->partials.p;
+  P.n_mv = pcg_mv_grid<T>(c);
+  P.up_part = c->partials_up.p;
   return P;
 }
 
@@ -686,6 +701,8 @@ void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, co
   }
   int maxgrid = std::max({c->grid_mv, c->grid_vec, c->grid_fan, c->grid_ft32, c->grid_geo});
   c->partials.alloc((size_t)maxgrid * 4);
+  c->partials_up.alloc((size_t)std::max(c->grid_upd, c->grid_vec) * 2);
+  c->partials_up.zero(s);
   c->counters.alloc(4);
   c->counters.zero(s);
   c->rr.alloc(4);
@@ -1111,13 +1128,20 @@ cfem_status cfem_profile_matvec(cfem_ctx *ctx, int32_t precision, int32_t n_laun
   return run_guarded([&]() -> cfem_status {
     check_ctx(ctx);
     if (n_launches <= 0) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "n_launches must be positive"};
-    // scalars that make the kernel take its full path: iteration > 0, beta = 1
+    // scalars that make the kernel take its full path: an update has run
+    // (u_iter 0) whose partials give r.z = 1 against gamma_prev = 1, so
+    // beta = 1, and no stopping rule fires
     Scalars h{};
     h.iter = 1;
-    h.gamma = h.gamma_prev = 1.0;
-    h.beta = 1.0;
+    h.u_iter = 0;
+    h.gamma = h.gamma_prev = h.gamma0 = 1.0;
+    h.alpha = h.beta = 1.0;
+    h.maxit = 1 << 30;
     Scalars *sc = ctx->sc.p + 2;
     CK(cudaMemcpyAsync(sc, &h, sizeof(Scalars), cudaMemcpyHostToDevice, ctx->stream));
+    ctx->partials_up.zero(ctx->stream);
+    static const double one[2] = {1.0, 1.0};
+    CK(cudaMemcpyAsync(ctx->partials_up.p, one, sizeof(one), cudaMemcpyHostToDevice, ctx->stream));
     const size_t ts = precision == CFEM_FP64 ? 8 : 4;
     auto run = [&](int n) {
       for (int i = 0; i < n; ++i) {

@@ -155,7 +155,8 @@ struct cfem_ctx {
   Vecs<float> v32;
   DBuf<double> io, tmp64, tmp64b, rr;
   DBuf<Scalars> sc;  // [0] FP64 solve, [1] FP32 solve, [2] misc counters
-  DBuf<double> partials;
+  DBuf<double> partials;     // grid-sum scratch; the PCG-form matvec's p.Ap partials
+  DBuf<double> partials_up;  // r.z, r.r partials of the PCG update kernel [grid][2]
   DBuf<unsigned int> counters;
   DBuf<int> err;
   Scalars *h_sc = nullptr;

@@ -39,10 +39,12 @@ struct Scalars {
   double rr, ff, tol;
   int rule, maxit, iter, done;  // done: 0 running, 1 converged, 2 diverged, 3 iteration cap
   unsigned int count_mv, count_up;
-  int pad0, pad1;
-  // alpha = gamma / sigma (set by the matvec's last block), beta = gamma / gamma_prev
-  // (set by the update's last block, 0 before the first direction): computed
-  // once, so no thread divides in FP64
+  int u_iter;  // iterations completed when the last update ran (-1: none since the init kernel)
+  int pad1;
+  // alpha = gamma / sigma (set by CTA 0 of the update from the matvec's block
+  // partials), beta = gamma / gamma_prev (set by CTA 0 of the matvec from the
+  // update's block partials, 0 before the first direction): every CTA derives
+  // them identically, so no thread divides differently
   double alpha, beta;
 };
 
@@ -271,6 +273,146 @@ __device__ __forceinline__ bool grid_sum_acc(DotAcc<T> (&a)[N], double (&v)[N], 
 }
 
 
+// ---- single-mesh PCG scalars without a last-block phase ---------------------
+// The PCG-form matvec and the update kernel of a single-mesh PCG pass their
+// grid sums as per-block partials only: each block stores its partial sums
+// (no fence, no ticket, no block waiting for the others), and every CTA of the
+// kernel that follows adds them after its dependency wait, in block order: the
+// same order in every CTA, so all CTAs derive bit-identical scalars. CTA 0
+// then publishes them for the kernel after it and for the host. A kernel
+// reads only Scalars fields that the kernel before it wrote:
+//   matvec reads  u_iter, gamma_prev, alpha (update) and the constants,
+//          writes gamma, rr, iter, beta, done;
+//   update reads  gamma, iter, done (matvec),
+//          writes alpha, sigma, gamma_prev, u_iter.
+// u_iter < 0 (init kernel): no update yet; the matvec takes the init kernel's
+// scalars and beta = 0.
+
+// Thread 0 stores the block totals of N accumulators at part[blockIdx.x * N + k]
+// (all threads call; red: N x 8 doubles of shared scratch).
+template <int N, typename T>
+__device__ __forceinline__ void store_block_partials(const DotAcc<T> (&a)[N], double *part, double *red) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    double w;
+    if constexpr (sizeof(T) == 8) {
+      w = a[k].s;
+      for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(0xffffffffu, w, o);
+    } else {
+      Comp32 c = a[k].c;
+      for (int o = 16; o > 0; o >>= 1) {
+        const float h2 = __shfl_down_sync(0xffffffffu, c.hi, o), l2 = __shfl_down_sync(0xffffffffu, c.lo, o);
+        c.merge(h2, l2);
+      }
+      w = (double)c.hi + (double)c.lo;
+    }
+    if (lane == 0) red[k * 8 + wid] = w;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      double t = 0;
+      for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += red[k * 8 + i];
+      part[(size_t)blockIdx.x * N + k] = t;
+    }
+  }
+}
+
+// First half of a fixed-order sum of per-block partials: thread t adds
+// part[b * N + k] for b = t, t + blockDim, ... in turn (two loads in flight),
+// a shuffle tree per warp, lane 0 stores the warp sum at red[k * 8 + warp].
+// After a barrier, partials_total() adds the warp sums in warp order. Blocks
+// of at most 256 threads.
+template <int N>
+__device__ __forceinline__ void partials_warp_sums(const double *part, int nblocks, double *red) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int B = blockDim.x;
+  double sum[N];
+#pragma unroll
+  for (int k = 0; k < N; ++k) sum[k] = 0;
+  for (int b0 = threadIdx.x; b0 < nblocks; b0 += 2 * B) {
+    double v[2][N];
+#pragma unroll
+    for (int q = 0; q < 2; ++q)
+#pragma unroll
+      for (int k = 0; k < N; ++k) v[q][k] = b0 + q * B < nblocks ? __ldcg(part + (size_t)(b0 + q * B) * N + k) : 0.0;
+#pragma unroll
+    for (int q = 0; q < 2; ++q)
+#pragma unroll
+      for (int k = 0; k < N; ++k)
+        if (b0 + q * B < nblocks) sum[k] += v[q][k];
+  }
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    double x = sum[k];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) red[k * 8 + wid] = x;
+  }
+}
+__device__ __forceinline__ double partials_total(const double *red, int k) {
+  double t = 0;
+  for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += red[k * 8 + i];
+  return t;
+}
+
+// Start of a single-mesh PCG-form matvec (all threads, after the dependency
+// wait): r.z and r.r of the update before it, beta and the stopping test
+// (reference rule gamma < tol gamma0, residual rule ||r|| <= tol ||f||, the
+// iteration cap). Returns true once the solve has stopped (uniform). Thread 0
+// alone reads the scalars, in the same round trip as every thread's partial
+// loads, and shares the result through red (24 doubles of shared scratch):
+// the CTAs of a grid reading the same line thread by thread would queue at
+// one L2 slice.
+template <typename T>
+__device__ __forceinline__ bool pcg_matvec_scalars(Scalars *s, const double *up_part, int n_up, T &beta,
+                                                   double *red) {
+  int ui = 0, done0 = 0, rule = 0, maxit = 0;
+  double alpha = 0, tol = 0, g0 = 0, ff = 0, gp = 1;
+  if (threadIdx.x == 0) {
+    ui = s->u_iter;
+    done0 = s->done;
+    alpha = s->alpha;
+    tol = s->tol;
+    g0 = s->gamma0;
+    ff = s->ff;
+    gp = s->gamma_prev;
+    rule = s->rule;
+    maxit = s->maxit;
+  }
+  partials_warp_sums<2>(up_part, n_up, red);  // (ignored before the first update)
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double b = 0;
+    int done = done0;
+    if (ui >= 0) {
+      const double g = partials_total(red, 0), rr = partials_total(red, 1);
+      const int it = ui + 1;
+      done = 0;
+      if (!isfinite(g) || !isfinite(alpha)) done = 2;
+      else if (rule == 0 && g < tol * g0) done = 1;
+      else if (rule == 1 && sqrt(rr) <= tol * sqrt(ff)) done = 1;
+      else if (it >= maxit) done = 3;
+      b = g / gp;
+      if (blockIdx.x == 0) {
+        s->gamma = g;
+        s->rr = rr;
+        s->iter = it;
+        s->beta = b;
+        s->done = done;
+      }
+    }
+    red[18] = b;
+    red[19] = (double)done;
+  }
+  __syncthreads();
+  beta = T(red[18]);
+  const bool stop = red[19] != 0.0;
+  __syncthreads();  // (red may be reused)
+  return stop;
+}
+
 // ------------------------------------------------------------------ element kernel
 // Stiffness (and consistent mass) action of one element in gradient form.
 // u[a][d]: masked nodal values; G: dim*dim gradient components of nodes 1..dim.
@@ -371,8 +513,10 @@ struct MvParams {
   const T *x3;       // DYN: a
   T *xout;           // PCG: p_new; DYN: d_new (owned nodes only)
   T *y;              // result accumulation (zero on entry)
-  Scalars *sc;       // PCG scalars (beta in, sigma out)
+  Scalars *sc;       // PCG scalars (single mesh)
   double *partials;  // [gridDim] partial sums of p.Ap
+  const double *up_part;  // PCG: r.z, r.r partials of the update before it, n_up blocks
+  int n_up;
   T c1, c2;          // DYN: d_new = d + c1 v + c2 a
   const uint16_t *inc, *inc_start;  // per-patch incidence lists (prep.hpp)
   int pe, np_max;    // element slots per patch, node slots per patch (multiple of 4)
@@ -438,9 +582,9 @@ __global__ void __launch_bounds__(kThreads) k_matvec(MvParams<T> P) {
   uint16_t *ss = si + 4 * P.pe;                                                // [np_max + 1] starts
   int32_t *sg = reinterpret_cast<int32_t *>(ss + ((P.np_max + 2) & ~1));       // [np_max] node ids
   uint8_t *sb = reinterpret_cast<uint8_t *>(sg + P.np_max);                    // [np_max] BC bits
-  if (MODE == MV_PCG && P.sc->done) return;
+  __shared__ double red_pcg[24];
   T beta = 0;
-  if (MODE == MV_PCG) beta = T(P.sc->beta);
+  if (MODE == MV_PCG && pcg_matvec_scalars<T>(P.sc, P.up_part, P.n_up, beta, red_pcg)) return;
   DotAcc<T> energy;
   for (int patch = blockIdx.x; patch < P.n_patches; patch += gridDim.x) {
     const int nb = P.node_off[patch], nn = P.node_off[patch + 1] - nb, own = P.own[patch];
@@ -557,13 +701,9 @@ __global__ void __launch_bounds__(kThreads) k_matvec(MvParams<T> P) {
     }
     __syncthreads();
   }
-  if (MODE == MV_PCG) {
-    DotAcc<T> ea[1] = {energy};
-    double v[1];
-    if (grid_sum_acc<1, T>(ea, v, P.partials, &P.sc->count_mv)) {
-      P.sc->sigma = v[0];
-      P.sc->alpha = P.sc->gamma / v[0];
-    }
+  if (MODE == MV_PCG) {  // p.Ap partials; the update kernel forms sigma and alpha
+    const DotAcc<T> ea[1] = {energy};
+    store_block_partials<1, T>(ea, P.partials, red_pcg);
   }
 }
 
@@ -582,7 +722,10 @@ struct VecParams {
   const T *dinv;
   const T *f;        // init: right-hand side
   Scalars *sc;
-  double *partials;
+  double *partials;  // init: grid-sum scratch
+  const double *mv_part;  // update: p.Ap partials of the matvec before it, n_mv blocks
+  int n_mv;
+  double *up_part;        // update: its own r.z, r.r partials [grid][2]
 };
 
 // r = f - u (warm) or f; x = 0 unless warm; z = M^-1 r; u = 0; gamma0 = r.z
@@ -620,6 +763,7 @@ __global__ void __launch_bounds__(kThreads) k_pcg_init(VecParams<T> P, int warm)
     s->rr = acc[1];
     s->ff = acc[2];
     s->iter = 0;
+    s->u_iter = -1;
     s->sigma = 0;
     s->alpha = 0;
     s->beta = 0;
@@ -635,18 +779,16 @@ __global__ void __launch_bounds__(kThreads) k_pcg_init(VecParams<T> P, int warm)
 template <typename T, int DIM>
 __global__ void __launch_bounds__(kThreads, 2) k_pcg_update(VecParams<T> P) {
   constexpr int VW = DIM == 3 ? 4 : 2;
-  griddep_wait();               // alpha and A p come from the matvec before it
+  griddep_wait();               // A p and the p.Ap partials come from the matvec before it
   griddep_launch_dependents();  // the next matvec may start streaming its blocks
-  Scalars *s = P.sc;
-  if (s->done) return;
-  const double alpha_d = s->alpha;
-  const T alpha = (T)alpha_d;
-  DotAcc<T> acc[2];
-  // U nodes per thread per round, all their loads issued before any is used
+  // U nodes per thread per round, all their loads issued before any is used;
+  // the first round's loads go out before the scalar exchange below, which
+  // they do not depend on
   constexpr int U = sizeof(T) == 4 ? 4 : 2;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x * U;
-  for (int64_t base = blockIdx.x * (int64_t)blockDim.x * U + threadIdx.x; base < P.n_nodes; base += stride) {
-    NodeV<T, VW> x[U], r[U], p[U], u[U], di[U];
+  int64_t base = blockIdx.x * (int64_t)blockDim.x * U + threadIdx.x;
+  NodeV<T, VW> x[U], r[U], p[U], u[U], di[U];
+  auto load_round = [&]() {
 #pragma unroll
     for (int q = 0; q < U; ++q) {
       const int64_t n = base + (int64_t)q * blockDim.x;
@@ -658,6 +800,39 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg_update(VecParams<T> P) {
         di[q] = ldv<T, VW>(P.dinv, n);
       }
     }
+  };
+  load_round();
+  // thread 0 reads the scalars while every thread loads the matvec's partials
+  // (see pcg_matvec_scalars); alpha = gamma / sigma in thread 0, shared
+  Scalars *s = P.sc;
+  __shared__ double red_pcg[24];
+  int done0 = 0, it0 = 0;
+  double gamma = 0;
+  if (threadIdx.x == 0) {
+    done0 = s->done;
+    gamma = s->gamma;
+    it0 = s->iter;
+  }
+  partials_warp_sums<1>(P.mv_part, P.n_mv, red_pcg);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double sig = partials_total(red_pcg, 0), a = gamma / sig;
+    red_pcg[18] = a;
+    red_pcg[19] = (double)done0;
+    if (blockIdx.x == 0 && !done0) {
+      s->sigma = sig;
+      s->alpha = a;
+      s->gamma_prev = gamma;
+      s->u_iter = it0;
+    }
+  }
+  __syncthreads();
+  if (red_pcg[19] != 0.0) return;
+  const double alpha_d = red_pcg[18];
+  const T alpha = (T)alpha_d;
+  DotAcc<T> acc[2];
+  for (bool first = true; base < P.n_nodes; base += stride, first = false) {
+    if (!first) load_round();
 #pragma unroll
     for (int q = 0; q < U; ++q) {
       const int64_t n = base + (int64_t)q * blockDim.x;
@@ -682,21 +857,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg_update(VecParams<T> P) {
       stv<T, VW>(P.u, n, zero);
     }
   }
-  double tot[2];
-  if (grid_sum_acc<2, T>(acc, tot, P.partials, &s->count_up)) {
-    const double *acc = tot;
-    s->gamma_prev = s->gamma;
-    s->gamma = acc[0];
-    s->beta = s->gamma / s->gamma_prev;
-    s->rr = acc[1];
-    s->iter += 1;
-    int done = 0;
-    if (!isfinite(acc[0]) || !isfinite(alpha_d)) done = 2;
-    else if (s->rule == 0 && acc[0] < s->tol * s->gamma0) done = 1;
-    else if (s->rule == 1 && sqrt(acc[1]) <= s->tol * sqrt(s->ff)) done = 1;
-    else if (s->iter >= s->maxit) done = 3;
-    s->done = done;
-  }
+  // r.z, r.r partials; the next matvec forms gamma, beta and the stopping test
+  store_block_partials<2, T>(acc, P.up_part, red_pcg);
 }
 
 }  // namespace cfem

@@ -40,9 +40,9 @@ __global__ void __launch_bounds__(kFanThreads) k_matvec_fan(MvParams<T> P, FanPa
   uint16_t *ss = si + kFanSlots * kFanThreads;                                         // [np_max + 1]
   int32_t *sg = reinterpret_cast<int32_t *>(ss + ((P.np_max + 2) & ~1));              // [np_max]
   uint8_t *sb = reinterpret_cast<uint8_t *>(sg + P.np_max);                            // [np_max]
-  if (MODE == MV_PCG && P.sc->done) return;
+  __shared__ double red_pcg[24];
   T beta = 0;
-  if (MODE == MV_PCG) beta = T(P.sc->beta);
+  if (MODE == MV_PCG && pcg_matvec_scalars<T>(P.sc, P.up_part, P.n_up, beta, red_pcg)) return;
   DotAcc<T> energy;
   for (int patch = blockIdx.x; patch < P.n_patches; patch += gridDim.x) {
     const int nb = P.node_off[patch], nn = P.node_off[patch + 1] - nb, own = P.own[patch];
@@ -181,13 +181,9 @@ __global__ void __launch_bounds__(kFanThreads) k_matvec_fan(MvParams<T> P, FanPa
     }
     __syncthreads();
   }
-  if (MODE == MV_PCG) {
-    DotAcc<T> ea[1] = {energy};
-    double v[1];
-    if (grid_sum_acc<1, T>(ea, v, P.partials, &P.sc->count_mv)) {
-      P.sc->sigma = v[0];
-      P.sc->alpha = P.sc->gamma / v[0];
-    }
+  if (MODE == MV_PCG) {  // p.Ap partials; the update kernel forms sigma and alpha
+    const DotAcc<T> ea[1] = {energy};
+    store_block_partials<1, T>(ea, P.partials, red_pcg);
   }
 }
 

@@ -246,7 +246,13 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
     for (int k = 0; k < 2; ++k)
       if (blockIdx.x + k * step < P.n_patches) issue_copy(blockIdx.x + k * step, k);
   griddep_wait();
-  if (MODE == MV_PCG && (batch ? P.bctl->all_done : P.sc->done)) {
+  // single mesh: beta and the stopping test from the update's partials (every
+  // CTA alike; the staging area, not in use yet, is the reduction scratch)
+  T beta = 0;
+  double *red_pcg = reinterpret_cast<double *>(sp);
+  const bool stopped = MODE == MV_PCG && (batch ? P.bctl->all_done != 0
+                                                : pcg_matvec_scalars<T>(P.sc, P.up_part, P.n_up, beta, red_pcg));
+  if (stopped) {
     if (threadIdx.x == 0 && !batch)  // let the copies issued above land before the CTA exits
       for (int k = 0; k < 2; ++k)
         if (blockIdx.x + k * step < P.n_patches) mbar_wait_bounded(&bar[k], 0u);
@@ -261,8 +267,6 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
       if (blockIdx.x + k * step < P.n_patches && patch_live(blockIdx.x + k * step))
         issue_copy(blockIdx.x + k * step, k);
   unsigned phase = 0;  // bit b: parity of the next completion of buffer b's barrier
-  T beta = 0;
-  if (MODE == MV_PCG && !batch) beta = T(P.sc->beta);
   // gathers of the node vectors of the patch in buffer Bq into stage st
   auto issue_gathers = [&](const unsigned char *Bq, T *st) {
     const int32_t *nq = reinterpret_cast<const int32_t *>(Bq + L.nodes_off);
@@ -579,13 +583,10 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
     }
   }
   griddep_launch_dependents();
-  if (MODE == MV_PCG && !batch) {
-    DotAcc<T> ea[1] = {energy};
-    double v[1];
-    if (grid_sum_acc<1, T>(ea, v, P.partials, &P.sc->count_mv)) {
-      P.sc->sigma = v[0];
-      P.sc->alpha = P.sc->gamma / v[0];
-    }
+  if (MODE == MV_PCG && !batch) {  // p.Ap partials; the update kernel forms sigma and alpha
+    // (every warp is past the last patch's compute phase: the staging area is free)
+    const DotAcc<T> ea[1] = {energy};
+    store_block_partials<1, T>(ea, P.partials, red_pcg);
   } else if (MODE == MV_PCG) {  // per-instance sigma and alpha from the per-patch sums
     __shared__ bool last;
     __threadfence();
