@@ -295,3 +295,34 @@ def test_autotune_patch_elems():
     u, _ = ctx.static_solve("fp64", tol=1e-14, stop_rule="residual")
     assert rel(u, xo) <= 1e-10
 
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_pcg_termination_3d(precision):
+    """Stopping paths of the 3D PCG (bulk-copy FP32 fan matvec, FP64 fan
+    matvec) whose scalars pass between the matvec and the update as block
+    partials: a zero right-hand side stops before the first update; an
+    iteration cap below, at and across the 16-iteration graph chunk stops at
+    exactly that count, on the same iterate as the oracle's PCG after as many
+    steps (so every alpha and beta of the recurrence agrees)."""
+    from cudafemproject_gb300 import capi
+    from cudafemproject_gb300.solver import FemContext
+    p = meshgen.box_3d(4, 4, 12, jitter=0.2, seed=4)
+    o = O.Oracle(p, consistent=True)
+    ctx = FemContext(p, semantics="consistent")
+    u, info = ctx.pcg(np.zeros(p.n_dof), precision, tol=1e-8, stop_rule="residual")
+    assert info["status"] == 0 and info["iterations"] == 0 and np.all(u == 0.0)
+    f = o.rhs()
+    tol = 1e-10 if precision == "fp64" else 2e-4
+    for m in (1, 2, 16, 17):
+        u, info = ctx.pcg(f, precision, tol=1e-30, stop_rule="residual", max_iter=m, allow_not_converged=True)
+        assert info["status"] == capi.ERR_NOT_CONVERGED and info["iterations"] == m, (m, info)
+        x, its = o.pcg(f, tol=1e-30, rule=1, maxit=m, allow_maxit=True)
+        assert its == m
+        assert rel(u, x) <= tol, (m, rel(u, x))
+    # and the same context still converges normally afterwards
+    u, info = ctx.pcg(f, precision, tol=1e-11 if precision == "fp64" else 1e-5, stop_rule="residual")
+    assert info["status"] == 0
+    if precision == "fp64":
+        x, _ = o.pcg(f, tol=1e-14, rule=1)
+        assert rel(u, x) <= 1e-7
