@@ -38,7 +38,7 @@ struct Scalars {
   double gamma, gamma_prev, gamma0, sigma;
   double rr, ff, tol;
   int rule, maxit, iter, done;  // done: 0 running, 1 converged, 2 diverged, 3 iteration cap
-  unsigned int count_mv, count_up;
+  unsigned int count_spare, count_up;  // count_up: grid-sum ticket of the init kernel
   int u_iter;  // iterations completed when the last update ran (-1: none since the init kernel)
   int pad1;
   // alpha = gamma / sigma (set by CTA 0 of the update from the matvec's block
