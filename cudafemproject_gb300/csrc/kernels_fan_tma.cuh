@@ -247,11 +247,14 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
       if (blockIdx.x + k * step < P.n_patches) issue_copy(blockIdx.x + k * step, k);
   griddep_wait();
   // single mesh: beta and the stopping test from the update's partials (every
-  // CTA alike; the staging area, not in use yet, is the reduction scratch)
+  // CTA alike; the staging area, not in use yet, is the reduction scratch).
+  // Stored-gradient blocks defer this to the first patch, after that patch's
+  // first gathers are on their way (they do not depend on beta).
   T beta = 0;
   double *red_pcg = reinterpret_cast<double *>(sp);
-  const bool stopped = MODE == MV_PCG && (batch ? P.bctl->all_done != 0
-                                                : pcg_matvec_scalars<T>(P.sc, P.up_part, P.n_up, beta, red_pcg));
+  const bool defer = MODE == MV_PCG && !GEO && !batch;
+  const bool stopped = MODE == MV_PCG && !defer &&
+                       (batch ? P.bctl->all_done != 0 : pcg_matvec_scalars<T>(P.sc, P.up_part, P.n_up, beta, red_pcg));
   if (stopped) {
     if (threadIdx.x == 0 && !batch)  // let the copies issued above land before the CTA exits
       for (int k = 0; k < 2; ++k)
@@ -350,19 +353,37 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
     // 1. stage node values: each thread issues the gathers of all its nodes
     //    (up to kStageUnroll) before using any of them
     constexpr int SU = kStageUnroll;
-    for (int i0 = threadIdx.x; i0 < nn; i0 += SU * kHfanThreads) {
-      NodeV<T, VW> v[SU], w[SU], a3[SU];
-      int gi[SU];
+    NodeV<T, VW> v[SU], w[SU], a3[SU];
+    int gi[SU];
+    auto stage_load = [&](int i0, bool with_w) {
 #pragma unroll
       for (int q = 0; q < SU; ++q) {
         const int i = i0 + q * kHfanThreads;
         gi[q] = i < nn ? nodes[i] : -1;
         if (gi[q] >= 0) {
           v[q] = ldv<T, VW>(P.x, gi[q]);
-          if ((MODE == MV_PCG && beta != T(0)) || MODE == MV_DYN) w[q] = ldv<T, VW>(P.x2, gi[q]);
+          if (with_w || MODE == MV_DYN) w[q] = ldv<T, VW>(P.x2, gi[q]);
           if (MODE == MV_DYN) a3[q] = ldv<T, VW>(P.x3, gi[q]);
         }
       }
+    };
+    int i0 = threadIdx.x;
+    bool loaded = false;
+    if (defer && it == 0) {
+      // first patch: this thread's first gathers, then the scalar exchange
+      // (uniform); the loaded values are combined once beta is known
+      stage_load(i0, true);
+      if (pcg_matvec_scalars<T>(P.sc, P.up_part, P.n_up, beta, red_pcg)) {
+        if (threadIdx.x == 0) {  // the copies issued above land before the CTA exits
+          if (!ok) mbar_wait_bounded(&bar[b], 0u);
+          if (patch + step < P.n_patches) mbar_wait_bounded(&bar[b ^ 1], (phase >> (b ^ 1)) & 1u);
+        }
+        return;
+      }
+      loaded = true;
+    }
+    for (; i0 < nn; i0 += SU * kHfanThreads, loaded = false) {
+      if (!loaded) stage_load(i0, MODE == MV_PCG && beta != T(0));
 #pragma unroll
       for (int q = 0; q < SU; ++q) {
         const int i = i0 + q * kHfanThreads;
