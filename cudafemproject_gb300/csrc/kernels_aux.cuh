@@ -218,8 +218,16 @@ __global__ void k_dyn_explicit(DynParams<T> P) {
   constexpr int VW = DIM == 3 ? 4 : 2;
   griddep_wait();               // y from the step's matvec
   griddep_launch_dependents();  // (the end-of-step kernel, then the next matvec)
-  const int step = P.st->step;
-  const T ca = (T)P.coef[2 * step], cb = (T)P.coef[2 * step + 1];
+  // thread 0 reads the step's load factors once per CTA (every thread reading
+  // the same line would queue at one L2 slice)
+  __shared__ T s_coef[2];
+  if (threadIdx.x == 0) {
+    const int step = P.st->step;
+    s_coef[0] = (T)P.coef[2 * step];
+    s_coef[1] = (T)P.coef[2 * step + 1];
+  }
+  __syncthreads();
+  const T ca = s_coef[0], cb = s_coef[1];
   for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < P.n_nodes; n += (int64_t)gridDim.x * blockDim.x) {
     NodeV<T, VW> y = ldv<T, VW>(P.y, n), fa = ldv<T, VW>(P.FA, n), fb = ldv<T, VW>(P.FB, n);
     NodeV<T, VW> mi = ldv<T, VW>(P.minv, n), a = ldv<T, VW>(P.a, n), v = ldv<T, VW>(P.v, n), zero;
@@ -241,8 +249,14 @@ __global__ void k_dyn_explicit(DynParams<T> P) {
 template <typename T, int DIM>
 __global__ void k_dyn_rhs(DynParams<T> P) {
   constexpr int VW = DIM == 3 ? 4 : 2;
-  const int step = P.st->step;
-  const T ca = (T)P.coef[2 * step], cb = (T)P.coef[2 * step + 1];
+  __shared__ T s_coef[2];  // (read once per CTA, see k_dyn_explicit)
+  if (threadIdx.x == 0) {
+    const int step = P.st->step;
+    s_coef[0] = (T)P.coef[2 * step];
+    s_coef[1] = (T)P.coef[2 * step + 1];
+  }
+  __syncthreads();
+  const T ca = s_coef[0], cb = s_coef[1];
   for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < P.n_nodes; n += (int64_t)gridDim.x * blockDim.x) {
     NodeV<T, VW> y = ldv<T, VW>(P.y, n), fa = ldv<T, VW>(P.FA, n), fb = ldv<T, VW>(P.FB, n), r, zero;
 #pragma unroll

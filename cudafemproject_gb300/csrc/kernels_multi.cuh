@@ -152,7 +152,13 @@ __global__ void __launch_bounds__(kHfanThreads, C <= 2 ? 3 : 2) k_matvec_multi(M
   T *fs = reinterpret_cast<T *>(smem_raw + S.fs);
   T *s_beta = reinterpret_cast<T *>(smem_raw + S.beta);
   int *s_done = reinterpret_cast<int *>(smem_raw + S.done);
-  if (MODE == MV_PCG && P.ctl->all_done) return;
+  if (MODE == MV_PCG) {  // (thread 0 reads the shared flag, see k_pcg_multi_vec)
+    if (threadIdx.x == 0) s_done[0] = P.ctl->all_done;
+    __syncthreads();
+    const bool all = s_done[0] != 0;
+    __syncthreads();
+    if (all) return;
+  }
   for (int c = threadIdx.x; c < K; c += blockDim.x) {
     s_en[c] = 0;
     s_done[c] = 0;
@@ -370,12 +376,23 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads) k_pcg_multi_vec(MultiParams<T> P, T *xv, T *r, T *z, const T *p, T *u,
                                                            const T *f, const T *dinv, int init) {
   constexpr int DIM = 3, VW = 4;
-  if (!init && P.ctl->all_done) return;
   const int K = P.K;
+  // the case scalars once per CTA (one thread per case), the shared flag by
+  // thread 0: every thread reading the same lines would queue at one L2 slice
+  __shared__ T s_alpha[kMaxCases];
+  __shared__ int s_frozen[kMaxCases], s_all;
+  if (threadIdx.x == 0) s_all = init ? 0 : P.ctl->all_done;
+  for (int cc = threadIdx.x; cc < K; cc += blockDim.x) {
+    const MultiScalars &sc = P.sc[cc];
+    const int fz = !init && sc.done;
+    s_frozen[cc] = fz;
+    s_alpha[cc] = init || fz ? T(0) : (T)sc.alpha;
+  }
+  __syncthreads();
+  if (s_all) return;
   const int c = threadIdx.x & (K - 1);
-  const MultiScalars &s = P.sc[c];
-  const bool frozen = !init && s.done;
-  const T alpha = init || frozen ? T(0) : (T)s.alpha;
+  const bool frozen = s_frozen[c] != 0;
+  const T alpha = s_alpha[c];
   DotAcc<T> acc[3];  // r.z, r.r, f.f
   const int64_t n_items = P.n_nodes * K;
   // U items per thread per round, all loads issued before any is used; the
