@@ -81,10 +81,12 @@ void set_pcg_vectors(cfem_ctx *c, const double *diag_op, const double *diag_pre)
   CKL();
 }
 
+// The explicit update with the end of the step fused in (receivers, step
+// counter through DynState::pstep, P.parity and P.dto set by the caller).
 template <typename T>
-void launch_dyn_explicit(cfem_ctx *c, const DynParams<T> &P) {
-  if (c->dim == 3) launch_pdl(k_dyn_explicit<T, 3>, dim3(c->grid_vec), dim3(kThreads), 0, c->stream, P);
-  else k_dyn_explicit<T, 2><<<c->grid_vec, kThreads, 0, c->stream>>>(P);
+void launch_dyn_explicit_step(cfem_ctx *c, const DynParams<T> &P) {
+  if (c->dim == 3) launch_pdl(k_dyn_explicit<T, 3, true>, dim3(c->grid_vec), dim3(kThreads), 0, c->stream, P);
+  else k_dyn_explicit<T, 2, true><<<c->grid_vec, kThreads, 0, c->stream>>>(P);
   CKL();
 }
 template <typename T>
@@ -129,6 +131,7 @@ cfem_status run_dyn(cfem_ctx *c, const cfem_dyn_params *prm, const cfem_wavelet 
   st.alloc(1);
   DynState hs{};
   hs.step = 1;
+  hs.pstep[0] = 1;  // explicit: the first step has parity 0
   CK(cudaMemcpyAsync(st.p, &hs, sizeof(hs), cudaMemcpyHostToDevice, c->stream));
   const int nrec = prm->n_receivers > 0 && prm->receiver_nodes && prm->receiver_trace ? prm->n_receivers : 0;
   DBuf<int32_t> recv;
@@ -224,7 +227,7 @@ cfem_status run_dyn(cfem_ctx *c, const cfem_dyn_params *prm, const cfem_wavelet 
   int status = CFEM_OK;
   T *dcur = d0.p, *dnext = d1.p;
   V.x.zero(c->stream);  // acceleration warm start / PCG solution
-  auto one_step = [&](T *from, T *to) {
+  auto one_step = [&](T *from, T *to, int parity) {
     mv.x = from;
     mv.xout = to;
     launch_mv<T>(c, MV_DYN, mv);
@@ -234,9 +237,10 @@ cfem_status run_dyn(cfem_ctx *c, const cfem_dyn_params *prm, const cfem_wavelet 
         k_invert<T><<<nblk(c->nvec), kThreads, 0, c->stream>>>(c->nvec, diag_pre.p, minv.p);
         CKL();
       }
-      launch_dyn_explicit<T>(c, dp);
-      launch_pdl(k_dyn_end_step<T>, dim3(1), dim3(kThreads), 0, c->stream, dp, (const T *)to, c->vw);
-      CKL();
+      DynParams<T> de = dp;
+      de.dto = to;
+      de.parity = parity;
+      launch_dyn_explicit_step<T>(c, de);
     }
   };
   if (expl) {
@@ -247,8 +251,8 @@ cfem_status run_dyn(cfem_ctx *c, const cfem_dyn_params *prm, const cfem_wavelet 
       cudaGraph_t g;
       CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
       try {
-        one_step(d0.p, d1.p);
-        one_step(d1.p, d0.p);
+        one_step(d0.p, d1.p, 0);
+        one_step(d1.p, d0.p, 1);
       } catch (...) {
         cudaGraph_t broken = nullptr;
         cudaStreamEndCapture(c->stream, &broken);
@@ -264,8 +268,8 @@ cfem_status run_dyn(cfem_ctx *c, const cfem_dyn_params *prm, const cfem_wavelet 
       // the resort swaps are captured: after an even number of steps slot_src is back in place
     }
     dcur = d0.p;
-    if (nsteps & 1) {
-      one_step(d0.p, d1.p);
+    if (nsteps & 1) {  // (after the pairs the next step's counter is pstep[0])
+      one_step(d0.p, d1.p, 0);
       dcur = d1.p;
     }
   } else {

@@ -51,7 +51,9 @@ struct Scalars {
 struct DynState {
   int step;
   unsigned int count;
-  int pad0, pad1;
+  // explicit steps in a two-step graph: the step of parity q reads pstep[q]
+  // and its CTA 0 writes pstep[q ^ 1] (no CTA reads what its own kernel writes)
+  int pstep[2];
 };
 
 // ------------------------------------------------------------------ helpers

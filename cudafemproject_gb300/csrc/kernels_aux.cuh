@@ -210,24 +210,36 @@ struct DynParams {
   int n_recv;
   double *trace;           // [steps][n_recv][dim]
   int dim;
+  const T *dto;            // explicit, end of step fused: the step's new displacements
+  int parity;              // explicit, end of step fused: the step's parity in the graph
 };
 
-// explicit: a_new = (F(t) - K d) / M ; v += (1-beta1) dt a_old + beta1 dt a_new
-template <typename T, int DIM>
+// explicit: a_new = (F(t) - K d) / M ; v += (1-beta1) dt a_old + beta1 dt a_new.
+// END_STEP: the step also ends here (receivers of P.dto recorded by CTA 0, the
+// step counter advanced through the parity pair of DynState) instead of in
+// k_dyn_end_step.
+template <typename T, int DIM, bool END_STEP = false>
 __global__ void k_dyn_explicit(DynParams<T> P) {
   constexpr int VW = DIM == 3 ? 4 : 2;
-  griddep_wait();               // y from the step's matvec
-  griddep_launch_dependents();  // (the end-of-step kernel, then the next matvec)
-  // thread 0 reads the step's load factors once per CTA (every thread reading
-  // the same line would queue at one L2 slice)
+  griddep_wait();               // y (and the new displacements) from the step's matvec
+  griddep_launch_dependents();  // (the end-of-step kernel or the next matvec)
+  // thread 0 reads the step and its load factors once per CTA (every thread
+  // reading the same line would queue at one L2 slice)
   __shared__ T s_coef[2];
+  __shared__ int s_step;
   if (threadIdx.x == 0) {
-    const int step = P.st->step;
+    const int step = END_STEP ? P.st->pstep[P.parity] : P.st->step;
+    s_step = step;
     s_coef[0] = (T)P.coef[2 * step];
     s_coef[1] = (T)P.coef[2 * step + 1];
   }
   __syncthreads();
   const T ca = s_coef[0], cb = s_coef[1];
+  if (END_STEP && blockIdx.x == 0)
+    for (int i = threadIdx.x; i < P.n_recv * P.dim; i += blockDim.x) {
+      const int r = i / P.dim, k = i % P.dim;
+      P.trace[((int64_t)(s_step - 1) * P.n_recv + r) * P.dim + k] = (double)P.dto[(int64_t)P.recv[r] * VW + k];
+    }
   for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < P.n_nodes; n += (int64_t)gridDim.x * blockDim.x) {
     NodeV<T, VW> y = ldv<T, VW>(P.y, n), fa = ldv<T, VW>(P.FA, n), fb = ldv<T, VW>(P.FB, n);
     NodeV<T, VW> mi = ldv<T, VW>(P.minv, n), a = ldv<T, VW>(P.a, n), v = ldv<T, VW>(P.v, n), zero;
@@ -243,6 +255,7 @@ __global__ void k_dyn_explicit(DynParams<T> P) {
     stv<T, VW>(P.v, n, v);
     stv<T, VW>(P.y, n, zero);
   }
+  if (END_STEP && blockIdx.x == 0 && threadIdx.x == 0) P.st->pstep[P.parity ^ 1] = s_step + 1;
 }
 
 // implicit: rhs = F(t) - K d ; y = 0
