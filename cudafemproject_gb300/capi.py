@@ -104,6 +104,7 @@ SIGNATURES = [
     ("cfem_profile_matvec", i32, [vp, i32, i32, C.POINTER(f64), C.POINTER(f64)]),
     ("cfem_matvec_energy_noalloc", i32, [vp, vp, vp, vp]),
     ("cfem_run_task", i32, [C.c_char_p, C.c_char_p, i32, vp, i64, C.POINTER(SolveInfo), C.POINTER(DynInfo)]),
+    ("cfem_write_vtk", i32, [C.c_char_p, i32, vp, i64, vp, i64, vp]),
 ]
 
 _lib = None

@@ -517,6 +517,28 @@ std::vector<std::string> readTaskList(const std::string &configPath) {
 }
 }  // namespace cfem_ref
 
+extern "C" CFEM_API cfem_status cfem_write_vtk(const char *path, int32_t dim, const double *nodes, int64_t n_nodes,
+                                               const int32_t *elems, int64_t n_elems, const float *u) {
+  try {
+    if (!path || (dim != 2 && dim != 3) || n_nodes < 0 || n_elems < 0 || (n_nodes && (!nodes || !u)) ||
+        (n_elems && !elems))
+      throw cfem_ref::Error(CFEM_ERR_INVALID_ARGUMENT, "bad cfem_write_vtk arguments");
+    std::vector<double> nv(nodes, nodes + n_nodes * dim);
+    std::vector<int32_t> ev(elems, elems + n_elems * (dim + 1));
+    cfem_ref::HostMatrix d((size_t)n_nodes, (size_t)dim);
+    std::copy(u, u + n_nodes * dim, d.get_data());
+    if (dim == 2) cfem_ref::MakeVTKfile2D(path, nv, ev, d);
+    else cfem_ref::MakeVTKfile3D(path, nv, ev, d);
+    return CFEM_OK;
+  } catch (const cfem_ref::Error &e) {
+    cfem_set_error_string(e.what());
+    return e.status;
+  } catch (const std::exception &e) {
+    cfem_set_error_string(e.what());
+    return CFEM_ERR_IO;
+  }
+}
+
 extern "C" CFEM_API cfem_status cfem_run_task(const char *config_path, const char *task, int32_t write_vtk,
                                               double *u_out, int64_t n_out, cfem_solve_info *static_info,
                                               cfem_dyn_info *dyn_info) {

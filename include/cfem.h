@@ -223,6 +223,13 @@ CFEM_API cfem_status cfem_adjoint(cfem_ctx *ctx, const cfem_solve_params *prm, c
  * receives the displacements. Keys under "gb300" select precision/semantics. */
 CFEM_API cfem_status cfem_run_task(const char *config_path, const char *task, int32_t write_vtk, double *u_out,
                                    int64_t n_out, cfem_solve_info *static_info, cfem_dyn_info *dyn_info);
+/* results.vtk of given data (host only, no GPU), in the layout of the
+ * reference's MakeVTKfile2D / MakeVTKfile3D (VTKfile.cpp:281-386): points
+ * (printed as float), cells, cell types, displacement vectors and their
+ * magnitudes. nodes [n_nodes][dim], elems [n_elems][dim + 1] (0-based),
+ * u [n_nodes][dim] in FP32 like the reference's displacement matrix. */
+CFEM_API cfem_status cfem_write_vtk(const char *path, int32_t dim, const double *nodes, int64_t n_nodes,
+                                    const int32_t *elems, int64_t n_elems, const float *u);
 /* Batched independent meshes (no counterpart in the reference, which solves
  * one mesh per process): n 3D meshes, each with its own material, in one
  * context. Node, element, constraint, load and face arrays are each mesh's

@@ -15,6 +15,7 @@
 //                     receiver text file -> SEG-Y by the reference's segyUtils convert()
 //
 // Every mode prints one JSON line on stdout with timings and counters.
+#include <VTKfile.h>
 #include <femfunc.h>
 #include <segyUtils.h>
 
@@ -59,6 +60,22 @@ int run_solve(bool dyn, const std::string &cfg, const std::string &task, const s
   write_bin(out, *dk.get_displacements());
   std::printf("{\"parse_s\": %.6f, \"solve_s\": %.6f, \"pcg_iterations\": %d, \"nodes\": %zu, \"elements\": %zu}\n",
               t1 - t0, t2 - t1, count_iterations(captured.str()), dk.get_nodesCount(), dk.get_elementsCount());
+  return 0;
+}
+
+// Static CPU solve, then the reference's own results writer (VTKfile.cpp
+// MakeVTKfile2D/3D) on the task's nodes, elements and displacements.
+int run_vtk(const std::string &cfg, const std::string &task, const std::string &out_vtk) {
+  dataKeeper dk(cfg, task);
+  std::stringstream captured;
+  std::streambuf *old = std::cout.rdbuf(captured.rdbuf());
+  gpuCalculateFEM_EbE_vec(CPU, dk, false);
+  if (dk.get_dim() == 2)
+    MakeVTKfile2D(out_vtk, *dk.get_nodes(), *dk.get_elementsIds(), *dk.get_displacements());
+  else
+    MakeVTKfile3D(out_vtk, *dk.get_nodes(), *dk.get_elementsIds(), *dk.get_displacements());
+  std::cout.rdbuf(old);
+  std::printf("{\"mode\": \"vtk\", \"nodes\": %zu, \"elements\": %zu}\n", dk.get_nodesCount(), dk.get_elementsCount());
   return 0;
 }
 
@@ -149,7 +166,7 @@ int run_iters(const std::string &cfg, const std::string &task, int k) {
 
 int main(int argc, char **argv) {
   if (argc < 5) {
-    std::fprintf(stderr, "usage: %s static|dyn|dump|iters <config.json> <task> <out|k>\n", argv[0]);
+    std::fprintf(stderr, "usage: %s static|dyn|dump|vtk|iters <config.json> <task> <out|k>\n", argv[0]);
     return 2;
   }
   std::string mode = argv[1];
@@ -170,6 +187,7 @@ int main(int argc, char **argv) {
   if (mode == "static") return run_solve(false, argv[2], argv[3], argv[4]);
   if (mode == "dyn") return run_solve(true, argv[2], argv[3], argv[4]);
   if (mode == "dump") return run_dump(argv[2], argv[3], argv[4]);
+  if (mode == "vtk") return run_vtk(argv[2], argv[3], argv[4]);
   if (mode == "iters") return run_iters(argv[2], argv[3], std::atoi(argv[4]));
   std::fprintf(stderr, "unknown mode %s\n", mode.c_str());
   return 2;

@@ -15,6 +15,9 @@ the reference checkout; the GPU tests only read the committed outputs).
 3. A seeded receiver text file and node list are converted to SEG-Y by the
    reference's segyUtils convert() (``ref_driver segy``); the three files are
    stored under segy/ (``--only segy`` regenerates just these).
+4. The reference's results writer (VTKfile.cpp MakeVTKfile2D/3D) writes the
+   static solution of sq8 and box3 (``ref_driver vtk``, the same CPU solve as
+   ref_static_<case>.npz); the files are stored under vtk/ (``--only vtk``).
 """
 from __future__ import annotations
 
@@ -105,13 +108,29 @@ def make_segy():
                    capture_output=True)
 
 
+def make_vtk():
+    """The reference's results.vtk of the static sq8 and box3 solutions."""
+    meshes = os.path.join(HERE, "meshes")
+    os.makedirs(os.path.join(HERE, "vtk"), exist_ok=True)
+    for name in ("sq8", "box3"):
+        d = CASES[name]["kind"] == "2d" and 2 or 3
+        p = make_problem(CASES[name])
+        with tempfile.TemporaryDirectory() as work:
+            shutil.copytree(os.path.join(meshes, f"{d}D"), os.path.join(work, "prepared_meshes", f"{d}D"))
+            cfg = write_cfg(work, d, p.E, p.nu)
+            run_driver("vtk", cfg, name, os.path.join(HERE, "vtk", f"{name}.vtk"))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--only", choices=["segy"], default=None)
+    ap.add_argument("--only", choices=["segy", "vtk"], default=None)
     args = ap.parse_args()
     if not os.path.exists(DRIVER):
         subprocess.run(["make", "-f", "oracle/ref.mk", f"REF={args.ref}/FEMproject", "-j8"], cwd=REPO, check=True)
+    if args.only == "vtk":
+        make_vtk()
+        return
     make_segy()
     if args.only == "segy":
         return
@@ -188,6 +207,7 @@ def main():
             np.savez(os.path.join(HERE, f"ref_{name}.npz"), u=u, pcg_iterations=info["pcg_iterations"],
                      **{k: v for k, v in spec.items() if k not in ("base", "wavelet")},
                      base=spec["base"], wavelet=json.dumps(spec["wavelet"]))
+    make_vtk()
     print("golden fixtures written to", HERE)
 
 

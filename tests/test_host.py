@@ -88,3 +88,26 @@ def test_abi_errors_without_gpu_work():
     assert L.cfem_create(C.byref(h), None, None, None, None) == capi.ERR_INVALID_ARGUMENT
     assert b"null" in L.cfem_last_error_string()
     assert L.cfem_dof_map(None, None) == capi.ERR_INVALID_ARGUMENT
+
+
+@pytest.mark.parametrize("name,dim", [("sq8", 2), ("box3", 3)])
+def test_vtk_writer_byte_exact(tmp_path, name, dim):
+    """results.vtk from cfem_write_vtk equals, byte for byte, the file the
+    reference's own writer (VTKfile.cpp MakeVTKfile2D/3D) produced for the same
+    mesh and the same FP32 displacements (the reference's CPU solve,
+    tests/golden/ref_static_<case>.npz and tests/golden/vtk/<case>.vtk)."""
+    import ctypes as C
+    from cudafemproject_gb300 import capi
+    from conftest import GOLDEN, golden_ref
+    p = golden_problem(name, dim)
+    u = np.ascontiguousarray(golden_ref(f"static_{name}")["u"], dtype=np.float32)
+    nodes = np.ascontiguousarray(p.nodes, dtype=np.float64)
+    elems = np.ascontiguousarray(p.elems, dtype=np.int32)
+    assert u.shape == (p.n_nodes, dim)
+    out = str(tmp_path / "results.vtk")
+    st = capi.lib().cfem_write_vtk(out.encode(), dim, nodes.ctypes.data, p.n_nodes, elems.ctypes.data, p.n_elems,
+                                   u.ctypes.data)
+    assert st == capi.OK
+    with open(out, "rb") as f, open(os.path.join(GOLDEN, "vtk", f"{name}.vtk"), "rb") as g:
+        assert f.read() == g.read()
+    assert capi.lib().cfem_write_vtk(out.encode(), 4, None, 0, None, 0, None) == capi.ERR_INVALID_ARGUMENT
