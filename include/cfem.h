@@ -21,7 +21,8 @@
  *    cudaMemcpyDefault on the context's stream).
  *  - One context per stream; no global mutable state besides the per-thread
  *    error string (replaces the reference's static cuBLAS handle,
- *    cuda_matrix.cpp:3-8).
+ *    cuda_matrix.cpp:3-8) and the one device scratch array shared by all
+ *    calls of cfem_matvec_energy_noalloc (see there).
  */
 #ifndef CFEM_H
 #define CFEM_H
@@ -308,11 +309,13 @@ CFEM_API cfem_status cfem_dyn_adjoint(cfem_ctx *ctx, const cfem_dyn_params *prm,
  * sums for at most CFEM_NOALLOC_MAX_BLOCKS blocks, about 33 KB, held on every
  * GPU that loads the library until the process exits). A context that needs
  * more blocks is rejected with CFEM_ERR_INVALID_ARGUMENT. The first call on a
- * device resolves the scratch address there; make that first call outside any
- * stream capture. All calls share the one scratch array, so calls that overlap
- * on the GPU (other streams, other threads, other contexts) race and must be
- * serialised by the caller. This entry point has no counterpart in the
- * reference. */
+ * device resolves the scratch address there. The call is synchronous: it
+ * waits for its own work on the context's stream before it returns (so that a
+ * host energy pointer holds the result), and so it cannot be recorded into a
+ * CUDA graph by stream capture. All calls share the one scratch array, so
+ * calls that overlap on the GPU (other streams, other threads, other
+ * contexts) race and must be serialised by the caller. This entry point has no
+ * counterpart in the reference. */
 #define CFEM_NOALLOC_MAX_BLOCKS 4096
 CFEM_API cfem_status cfem_matvec_energy_noalloc(cfem_ctx *ctx, const double *x, double *y, double *energy);
 /* Per-element Young's modulus update (keeps geometry; rebuilds operator scale). */

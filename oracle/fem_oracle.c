@@ -154,6 +154,10 @@ struct orc_ctx {
   double *fscale;   /* consistent traction factor per face: L/2 (2D) or A/3 (3D) */
   double rho, E;
   int32_t *ctype;   /* per-node constraint code or 0 */
+  /* optional assembled copy of K' in dim x dim node blocks (orc_assemble) */
+  int64_t *bptr;    /* nn+1 row starts (node rows) */
+  int32_t *bcol;    /* block column nodes, ascending per row */
+  double *bval;     /* [block][dim][dim] */
 };
 
 int64_t orc_ndof(const orc_ctx *c) { return c->nd; }
@@ -239,6 +243,7 @@ void orc_free(orc_ctx *c) {
   ebe_free_f64(&c->m);
   free(c->Ee); free(c->vol); free(c->diag); free(c->yloc); free(c->Floc); free(c->press); free(c->press0);
   free(c->fscale); free(c->ctype);
+  free(c->bptr); free(c->bcol); free(c->bval);
   free(c);
 }
 
@@ -259,9 +264,101 @@ void orc_get_element_matrices(const orc_ctx *c, double *ke) {
 
 void orc_get_diag(const orc_ctx *c, double *d) { memcpy(d, c->diag, sizeof(double) * c->nd); }
 
+static int cmp_i32(const void *a, const void *b) {
+  const int32_t x = *(const int32_t *)a, y = *(const int32_t *)b;
+  return (x > y) - (x < y);
+}
+
+/* Node neighbours of node i (itself included), sorted and unique; returns the count. */
+static int64_t node_row(const orc_ctx *c, const int64_t *eptr, const int32_t *elist, int64_t i, int32_t *buf) {
+  const int nv = c->nv;
+  int64_t n = 0;
+  for (int64_t k = eptr[i]; k < eptr[i + 1]; ++k)
+    for (int b = 0; b < nv; ++b) buf[n++] = c->m.el[(int64_t)elist[k] * nv + b];
+  qsort(buf, (size_t)n, sizeof(int32_t), cmp_i32);
+  int64_t u = 0;
+  for (int64_t k = 0; k < n; ++k)
+    if (u == 0 || buf[k] != buf[u - 1]) buf[u++] = buf[k];
+  return u;
+}
+
+int orc_assemble(orc_ctx *c) {
+  const int dim = c->dim, nv = c->nv, w = c->w, bs = dim * dim;
+  const int64_t nn = c->nn, ne = c->ne;
+  if (c->bptr) return 0;
+  /* node -> incident elements, in element order */
+  int64_t *eptr = (int64_t *)calloc((size_t)nn + 1, sizeof(int64_t));
+  int32_t *elist = (int32_t *)malloc(sizeof(int32_t) * (size_t)(ne * nv));
+  for (int64_t e = 0; e < ne; ++e)
+    for (int a = 0; a < nv; ++a) eptr[c->m.el[e * nv + a] + 1]++;
+  int maxdeg = 0;
+  for (int64_t i = 0; i < nn; ++i) {
+    if (eptr[i + 1] > maxdeg) maxdeg = (int)eptr[i + 1];
+    eptr[i + 1] += eptr[i];
+  }
+  int64_t *fill = (int64_t *)malloc(sizeof(int64_t) * (size_t)nn);
+  memcpy(fill, eptr, sizeof(int64_t) * (size_t)nn);
+  for (int64_t e = 0; e < ne; ++e)
+    for (int a = 0; a < nv; ++a) elist[fill[c->m.el[e * nv + a]]++] = (int32_t)e;
+  free(fill);
+  c->bptr = (int64_t *)calloc((size_t)nn + 1, sizeof(int64_t));
+  const size_t bufn = (size_t)maxdeg * nv + 1;
+#pragma omp parallel
+  {
+    int32_t *buf = (int32_t *)malloc(sizeof(int32_t) * bufn);
+#pragma omp for schedule(static)
+    for (int64_t i = 0; i < nn; ++i) c->bptr[i + 1] = node_row(c, eptr, elist, i, buf);
+    free(buf);
+  }
+  for (int64_t i = 0; i < nn; ++i) c->bptr[i + 1] += c->bptr[i];
+  c->bcol = (int32_t *)malloc(sizeof(int32_t) * (size_t)(c->bptr[nn] > 0 ? c->bptr[nn] : 1));
+  c->bval = (double *)calloc((size_t)c->bptr[nn] * bs + 1, sizeof(double));
+  /* each row sums its blocks over its incident elements in element order */
+#pragma omp parallel
+  {
+    int32_t *buf = (int32_t *)malloc(sizeof(int32_t) * bufn);
+#pragma omp for schedule(static)
+    for (int64_t i = 0; i < nn; ++i) {
+      const int64_t r0 = c->bptr[i], n = node_row(c, eptr, elist, i, buf);
+      memcpy(c->bcol + r0, buf, sizeof(int32_t) * (size_t)n);
+      for (int64_t k = eptr[i]; k < eptr[i + 1]; ++k) {
+        const int64_t e = elist[k];
+        const double *K = c->m.K + e * w * w; /* column-major: K[row + col * w] */
+        int a = 0;
+        while (c->m.el[e * nv + a] != i) ++a;
+        for (int b = 0; b < nv; ++b) {
+          const int32_t j = c->m.el[e * nv + b];
+          const int32_t *hit = (const int32_t *)bsearch(&j, c->bcol + r0, (size_t)n, sizeof(int32_t), cmp_i32);
+          double *blk = c->bval + (r0 + (hit - (c->bcol + r0))) * bs;
+          for (int di = 0; di < dim; ++di)
+            for (int dj = 0; dj < dim; ++dj) blk[di * dim + dj] += K[(dim * a + di) + (dim * b + dj) * w];
+        }
+      }
+    }
+    free(buf);
+  }
+  free(eptr);
+  free(elist);
+  return 0;
+}
+
 void orc_matvec(const orc_ctx *c, const double *x, double *y) {
   const int w = c->w;
   const ebe_f64 *m = &c->m;
+  if (c->bptr) {
+    const int dim = c->dim, bs = dim * dim;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < c->nn; ++i) {
+      double acc[3] = {0, 0, 0};
+      for (int64_t k = c->bptr[i]; k < c->bptr[i + 1]; ++k) {
+        const double *blk = c->bval + k * bs, *xj = x + (int64_t)dim * c->bcol[k];
+        for (int di = 0; di < dim; ++di)
+          for (int dj = 0; dj < dim; ++dj) acc[di] += blk[di * dim + dj] * xj[dj];
+      }
+      for (int di = 0; di < dim; ++di) y[(int64_t)dim * i + di] = acc[di];
+    }
+    return;
+  }
 #pragma omp parallel for schedule(static)
   for (int64_t e = 0; e < c->ne; ++e) {
     double xe[12];
@@ -359,6 +456,7 @@ static int pcg_generic(const orc_ctx *c, orc_op op, void *user, const double *di
     memset(x, 0, sizeof(double) * n);
     memcpy(r, f, sizeof(double) * n);
   }
+#pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < n; ++i) z[i] = r[i] / dinv_src[i];
   memcpy(pp, z, sizeof(double) * n);
   double g0 = dsum_blocks(r, z, n), g = g0;
@@ -370,6 +468,7 @@ static int pcg_generic(const orc_ctx *c, orc_op op, void *user, const double *di
     ++it;
     op(c, pp, u, user);
     double sg = dsum_blocks(pp, u, n), alpha = g / sg;
+#pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; ++i) { x[i] += alpha * pp[i]; r[i] -= alpha * u[i]; z[i] = r[i] / dinv_src[i]; }
     double gn = dsum_blocks(r, z, n);
     if (rule == 0 && gn < tol * g0) break;
@@ -377,6 +476,7 @@ static int pcg_generic(const orc_ctx *c, orc_op op, void *user, const double *di
     if (!isfinite(gn)) { rc = -3; break; }
     if (it >= maxit) { rc = -4; break; }
     double beta = gn / g;
+#pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; ++i) pp[i] = z[i] + beta * pp[i];
     g = gn;
   }
@@ -391,7 +491,92 @@ int orc_pcg(const orc_ctx *c, const double *f, double *x, double tol, int32_t ru
   return pcg_generic(c, op_k, NULL, c->diag, f, x, 0, tol, rule, maxit, iters);
 }
 
+int orc_pcg_warm(const orc_ctx *c, const double *f, double *x, double tol, int32_t rule, int32_t maxit,
+                 int32_t *iters) {
+  return pcg_generic(c, op_k, NULL, c->diag, f, x, 1, tol, rule, maxit, iters);
+}
+
 /* Element mass blocks: lumped (per DOF) or consistent (w x w, same-component coupling). */
+/* The same FP32 port, set up once and then timed in samples of k iterations
+ * (the reference arm of the benchmark times one sample per step). */
+struct orc_ebe_timer {
+  ebe_f32 m;
+  cgm_f32 v;
+  float gamma;
+  int64_t n;
+  double setup_s, init_s;
+};
+
+int orc_ebe_timer_create(const orc_problem *p, orc_ebe_timer **out) {
+  orc_ebe_timer *t = (orc_ebe_timer *)calloc(1, sizeof(orc_ebe_timer));
+  double t0 = wall_s();
+  int rc = ebe_init_f32(&t->m, p);
+  if (rc) { ebe_free_f32(&t->m); free(t); return rc; }
+  ebe_f32 *m = &t->m;
+  const int64_t n = m->ne * m->w;
+  t->n = n;
+  ebe_klocals_f32(m);
+  float *diag = (float *)malloc(sizeof(float) * n);
+  for (int64_t e = 0; e < m->ne; ++e)
+    for (int j = 0; j < m->w; ++j) diag[e * m->w + j] = m->K[e * m->w * m->w + m->w * j + j];
+  ebe_face_lengths_f32(m);
+  ebe_flocals_f32(m, NULL, 0.f);
+  cgm_alloc_f32(&t->v, n);
+  memcpy(t->v.r, m->Fl, sizeof(float) * n);
+  double t1 = wall_s();
+  ebe_asm_gather_f32(m, diag, t->v.mm);
+  for (int64_t i = 0; i < n; ++i) t->v.z[i] = t->v.r[i] / t->v.mm[i];
+  ebe_asm_gather_f32(m, t->v.z, t->v.s);
+  t->gamma = ebe_dot_f32(t->v.r, t->v.s, n);
+  memcpy(t->v.p, t->v.s, sizeof(float) * n);
+  free(diag);
+  t->setup_s = t1 - t0;
+  t->init_s = wall_s() - t1;
+  *out = t;
+  return 0;
+}
+
+/* k more iterations of the loop body of ebe_pcg_f32 (no stopping test);
+ * returns their wall time in seconds. */
+double orc_ebe_timer_iters(orc_ebe_timer *t, int32_t k) {
+  ebe_f32 *m = &t->m;
+  cgm_f32 *v = &t->v;
+  const int64_t n = t->n;
+  double t0 = wall_s();
+  for (int it = 0; it < k; ++it) {
+    ebe_bmm_f32(m, v->p, v->u);
+    float sum = ebe_dot_f32(v->p, v->u, n), alpha = t->gamma / sum;
+    ebe_axpby_f32(v->x, 1.f, v->p, alpha, n);
+    ebe_axpby_f32(v->r, 1.f, v->u, -1.f * alpha, n);
+    for (int64_t i = 0; i < n; ++i) v->z[i] = v->r[i] / v->mm[i];
+    ebe_asm_gather_f32(m, v->z, v->s);
+    float gnew = ebe_dot_f32(v->r, v->s, n);
+    ebe_axpby_f32(v->p, gnew / t->gamma, v->s, 1.f, n);
+    t->gamma = gnew;
+  }
+  return wall_s() - t0;
+}
+
+void orc_ebe_timer_info(const orc_ebe_timer *t, double *setup_s, double *init_s) {
+  if (setup_s) *setup_s = t->setup_s;
+  if (init_s) *init_s = t->init_s;
+}
+
+void orc_ebe_timer_free(orc_ebe_timer *t) {
+  if (!t) return;
+  cgm_free_f32(&t->v);
+  ebe_free_f32(&t->m);
+  free(t);
+}
+
+int orc_num_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
 static void mass_coeffs(const orc_ctx *c, int64_t e, int lumped, double *md, double *mo) {
   /* md: diagonal (or lumped) entry, mo: same-component off-diagonal entry */
   double mass = c->rho * c->vol[e];

@@ -79,6 +79,15 @@ int orc_ebe_setup_f32(const orc_problem *p, const orc_wavelet *w, float *mask, f
 /* Wall-clock of setup and of k PCG iterations (FP32, single thread): the CPU baseline leg. */
 int orc_ebe_time_f32(const orc_problem *p, int32_t k, double *setup_s, double *iter_s);
 
+/* The same port set up once, then timed in samples of k PCG iterations. */
+typedef struct orc_ebe_timer orc_ebe_timer;
+int orc_ebe_timer_create(const orc_problem *p, orc_ebe_timer **out);
+double orc_ebe_timer_iters(orc_ebe_timer *t, int32_t k);
+void orc_ebe_timer_info(const orc_ebe_timer *t, double *setup_s, double *init_s);
+void orc_ebe_timer_free(orc_ebe_timer *t);
+/* OpenMP threads the FP64 form uses (1 without OpenMP). */
+int orc_num_threads(void);
+
 /* ---- FP64 global-vector form ------------------------------------------------ */
 typedef struct orc_ctx orc_ctx;
 int orc_setup(const orc_problem *p, orc_ctx **out);
@@ -96,12 +105,20 @@ void orc_get_element_matrices(const orc_ctx *c, double *ke);
 void orc_get_diag(const orc_ctx *c, double *d);
 /* Global right-hand side at time t (initFlocals / calcFlocals then assembly). */
 void orc_get_rhs(orc_ctx *c, const orc_wavelet *w, double t, double *f);
+/* Assembles K' once into dim x dim node blocks (the same element matrices,
+ * summed per node pair in element order); orc_matvec then multiplies with the
+ * assembled copy, which reads about a quarter of the bytes of the element
+ * matrices on tet meshes. Call it before any solve it should speed up. */
+int orc_assemble(orc_ctx *c);
 /* y = K' x, K' the constrained stiffness. */
 void orc_matvec(const orc_ctx *c, const double *x, double *y);
 /* Jacobi PCG from x = 0. rule 0: stop when gamma < tol*gamma0 (reference rule,
  * gamma = r.M^-1.r); rule 1: stop when ||r||_2 <= tol*||f||_2 (recursive r). */
 int orc_pcg(const orc_ctx *c, const double *f, double *x, double tol, int32_t rule, int32_t maxit,
             int32_t *iters);
+/* The same, starting from the x passed in (rule 1 compares ||f - K'x|| with tol*||f||). */
+int orc_pcg_warm(const orc_ctx *c, const double *f, double *x, double tol, int32_t rule, int32_t maxit,
+                 int32_t *iters);
 /* Dynamics (GN22), compat or consistent per the problem flag. pcg_tol/pcg_rule
  * are used by the implicit scheme (compat uses rule 0, tol 1e-4 like the reference). */
 int orc_dyn_run(orc_ctx *c, const orc_wavelet *w, const orc_dyn *d, double pcg_tol, int32_t pcg_rule,

@@ -70,6 +70,15 @@ def lib():
         L.orc_ebe_setup_f32.argtypes = [P, W] + [C.c_void_p] * 6
         L.orc_ebe_time_f32.argtypes = [P, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.orc_setup.argtypes = [P, C.POINTER(C.c_void_p)]
+        L.orc_assemble.argtypes = [C.c_void_p]
+        L.orc_pcg_warm.argtypes = [C.c_void_p, _f64p, _f64p, C.c_double, C.c_int32, C.c_int32,
+                                   C.POINTER(C.c_int32)]
+        L.orc_ebe_timer_create.argtypes = [P, C.POINTER(C.c_void_p)]
+        L.orc_ebe_timer_iters.restype = C.c_double
+        L.orc_ebe_timer_iters.argtypes = [C.c_void_p, C.c_int32]
+        L.orc_ebe_timer_info.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.orc_ebe_timer_free.argtypes = [C.c_void_p]
+        L.orc_num_threads.restype = C.c_int
         L.orc_free.argtypes = [C.c_void_p]
         L.orc_ndof.restype = C.c_int64
         L.orc_ndof.argtypes = [C.c_void_p]
@@ -170,6 +179,37 @@ def ebe_time(p, k):
     return s.value, i.value
 
 
+def num_threads() -> int:
+    return int(lib().orc_num_threads())
+
+
+class EbeTimer:
+    """The FP32 port of the reference's PCG, set up once and timed in samples
+    of k iterations (the reference arm of the benchmark)."""
+
+    def __init__(self, p):
+        self._pk = _Packed(p, False)
+        self._h = C.c_void_p()
+        rc = lib().orc_ebe_timer_create(C.byref(self._pk.s), C.byref(self._h))
+        if rc:
+            raise RuntimeError(f"oracle timer setup failed: {rc}")
+        s, i = C.c_double(0), C.c_double(0)
+        lib().orc_ebe_timer_info(self._h, C.byref(s), C.byref(i))
+        self.setup_s, self.init_s = s.value, i.value
+
+    def iters(self, k: int) -> float:
+        """Wall seconds of k more PCG iterations."""
+        return float(lib().orc_ebe_timer_iters(self._h, int(k)))
+
+    def close(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.orc_ebe_timer_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
 class Oracle:
     """FP64 global-vector oracle (compat or consistent)."""
 
@@ -187,6 +227,14 @@ class Oracle:
         if getattr(self, "_h", None) and _lib is not None:
             _lib.orc_free(self._h)
             self._h = None
+
+    def assemble(self):
+        """Switch matvecs and solves to the assembled node-block copy of K'
+        (same element matrices, other summation order: large meshes)."""
+        rc = lib().orc_assemble(self._h)
+        if rc:
+            raise RuntimeError(f"oracle assemble failed: {rc}")
+        return self
 
     def mask(self):
         m = np.zeros(self.p.n_elems * self.w, np.int32)
@@ -229,6 +277,16 @@ class Oracle:
         rc = lib().orc_pcg(self._h, np.ascontiguousarray(f, np.float64), x, float(tol), int(rule), int(maxit),
                            C.byref(it))
         if rc not in ((0, -4) if allow_maxit else (0,)):
+            raise RuntimeError(f"oracle pcg failed: {rc}")
+        return x, it.value
+
+    def pcg_warm(self, f, x0, tol=1e-12, rule=1, maxit=1000000):
+        """Jacobi PCG from the iterate x0 (returns a new array)."""
+        x = np.array(x0, dtype=np.float64, copy=True)
+        it = C.c_int32(0)
+        rc = lib().orc_pcg_warm(self._h, np.ascontiguousarray(f, np.float64), x, float(tol), int(rule), int(maxit),
+                                C.byref(it))
+        if rc:
             raise RuntimeError(f"oracle pcg failed: {rc}")
         return x, it.value
 

@@ -4,13 +4,14 @@
 # shipped or measured as the product; the binary is used by tests (FP32 cross
 # check of the oracle) and as the CPU baseline where it can be built.
 #
-#   make -f oracle/ref.mk REF=/root/reference/FEMproject
+#   make -f oracle/ref.mk REF=<reference checkout>/FEMproject
+#   (or CFEM_REFERENCE_ROOT=<reference checkout> make -f oracle/ref.mk)
 #
 # Outputs go to oracle/_ref/ only (git-ignored). The reference's own CMake
 # build is not used; its CUDA backend is left out (WITH_CUDA undefined), which
 # is exactly the DEVICE_NAME == CPU path of femfunc.cpp.
 
-REF ?= /root/reference/FEMproject
+REF ?= $(CFEM_REFERENCE_ROOT)/FEMproject
 OUT ?= oracle/_ref
 CXX ?= g++
 # -ffp-contract=off: no FMA contraction, so x86 and aarch64 round alike.

@@ -1,7 +1,7 @@
 """Regenerates the golden fixtures in tests/golden/ (run in a container that has
 the reference checkout; the GPU tests only read the committed outputs).
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    CFEM_REFERENCE_ROOT=<reference checkout> python tests/golden/make_golden.py [--ref <checkout>]
 
 1. The reference's own LS-DYNA parser (mesh_parser_lib/fem_parser.py) turns
    raw_meshes/2D/{test_rect_pcg,9task_3}.k into prepared meshes (the committed
@@ -123,9 +123,12 @@ def make_vtk():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("CFEM_REFERENCE_ROOT"),
+                    help="reference checkout (default: $CFEM_REFERENCE_ROOT)")
     ap.add_argument("--only", choices=["segy", "vtk"], default=None)
     args = ap.parse_args()
+    if not args.ref:
+        ap.error("the reference checkout is needed: --ref or CFEM_REFERENCE_ROOT")
     if not os.path.exists(DRIVER):
         subprocess.run(["make", "-f", "oracle/ref.mk", f"REF={args.ref}/FEMproject", "-j8"], cwd=REPO, check=True)
     if args.only == "vtk":

@@ -9,11 +9,15 @@ import pytest
 from conftest import GOLDEN
 from cudafemproject_gb300 import kfile, meshgen, meshio
 
-REF_RAW = "/root/reference/raw_meshes/2D"
+# the reference checkout (moarseniy/CudaFEMproject), where one is present
+REF_ROOT = os.environ.get("CFEM_REFERENCE_ROOT", "")
+REF_RAW = os.path.join(REF_ROOT, "raw_meshes", "2D") if REF_ROOT else ""
 
 
 @pytest.mark.parametrize("task", ["test_rect_pcg", "9task_3"])
 def test_reference_raw_meshes_give_the_golden_prepared_meshes(task, tmp_path):
+    if not REF_RAW:
+        pytest.skip("CFEM_REFERENCE_ROOT (reference checkout) not set")
     raw = os.path.join(REF_RAW, task + ".k")
     if not os.path.exists(raw):
         pytest.skip("reference raw meshes not present")

@@ -93,3 +93,54 @@ def test_consistent_traction_total_force():
     f = O.Oracle(p, consistent=True).rhs().reshape(-1, 3)
     assert abs(f[:, 1].sum() - (-1e3 * 1.0 * 1.0)) < 1e-6
     assert abs(f[:, 0].sum()) < 1e-9
+
+
+@pytest.mark.parametrize("name,dim", STATIC_CASES)
+def test_assembled_form_equals_element_form(name, dim):
+    """The node-block copy of K' (orc_assemble) multiplies like the element
+    matrices and solves to the same answer, compat and consistent."""
+    p = golden_problem(name, dim)
+    for consistent in (False, True):
+        o = O.Oracle(p, consistent=consistent)
+        x = np.random.default_rng(3).standard_normal(o.ndof)
+        y0 = o.matvec(x)
+        f = o.rhs()
+        u0, it0 = o.pcg(f, tol=1e-13, rule=1)
+        o.assemble()
+        assert rel(o.matvec(x), y0) < 1e-14
+        u1, it1 = o.pcg(f, tol=1e-13, rule=1)
+        assert rel(u1, u0) < 1e-11
+        assert abs(it1 - it0) <= 2
+
+
+def test_assembled_form_jittered_box_with_young_field():
+    from cudafemproject_gb300 import meshgen
+    p = meshgen.box_3d(4, 5, 12, jitter=0.2, seed=4)
+    p.elem_E = 2e7 * np.exp(0.5 * np.random.default_rng(5).standard_normal(p.n_elems))
+    o = O.Oracle(p, consistent=True)
+    x = np.random.default_rng(6).standard_normal(o.ndof)
+    y0 = o.matvec(x)
+    o.assemble()
+    assert rel(o.matvec(x), y0) < 1e-14
+
+
+def test_warm_pcg_continues_to_tighter_tolerance():
+    from cudafemproject_gb300 import meshgen
+    p = meshgen.box_3d(4, 4, 16, jitter=0.2, seed=1)
+    o = O.Oracle(p, consistent=True).assemble()
+    f = o.rhs()
+    xc, _ = o.pcg(f, tol=1e-13, rule=1)
+    x6, _ = o.pcg(f, tol=1e-6, rule=1)
+    xw, itw = o.pcg_warm(f, x6, tol=1e-13, rule=1)
+    assert itw > 0
+    assert rel(xw, xc) < 1e-11
+
+
+def test_ebe_timer_runs_the_port_loop():
+    from cudafemproject_gb300 import meshgen
+    p = meshgen.box_3d(3, 3, 12)
+    t = O.EbeTimer(p)
+    assert t.setup_s >= 0 and t.init_s >= 0
+    assert t.iters(3) >= 0
+    t.close()
+    assert O.num_threads() >= 1

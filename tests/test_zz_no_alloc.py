@@ -51,6 +51,32 @@ def test_noalloc_matches_allocating_matvec(dim):
         assert abs(e_host.value - e_ref) <= 1e-12 * abs(e_ref), call
 
 
+def test_noalloc_allocates_no_device_memory():
+    """After a first call (which resolves the scratch address on this device),
+    further calls leave both the device's free memory and torch's allocator
+    untouched, with device and host energy pointers."""
+    torch = pytest.importorskip("torch")
+    from cudafemproject_gb300.solver import FemContext
+    p = meshgen.box_3d(5, 5, 12, jitter=0.2, seed=3)
+    ctx = FemContext(p)
+    L = capi.lib()
+    x = torch.tensor(np.random.default_rng(1).standard_normal(p.n_dof), device="cuda")
+    y = torch.empty_like(x)
+    e_dev = torch.zeros(1, dtype=torch.float64, device="cuda")
+    e_host = C.c_double(0.0)
+    args = lambda e: (ctx._h, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), e)
+    capi.check(L.cfem_matvec_energy_noalloc(*args(C.c_void_p(e_dev.data_ptr()))), "warm-up")
+    torch.cuda.synchronize()
+    free0, alloc0 = torch.cuda.mem_get_info()[0], torch.cuda.memory_allocated()
+    for _ in range(3):
+        capi.check(L.cfem_matvec_energy_noalloc(*args(C.c_void_p(e_dev.data_ptr()))), "device energy")
+        capi.check(L.cfem_matvec_energy_noalloc(*args(C.byref(e_host))), "host energy")
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert torch.cuda.memory_allocated() == alloc0
+    assert e_host.value == e_dev.item()
+
+
 def test_noalloc_rejects_bad_arguments():
     from cudafemproject_gb300.solver import FemContext
     ctx = FemContext(meshgen.square_2d(4))
