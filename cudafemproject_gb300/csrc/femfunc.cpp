@@ -395,6 +395,58 @@ void gpuPCG_EbE_vec(std::vector<double> &displacements, DEVICE_NAME, dataKeeper 
   check(st, "gpuPCG_EbE_vec");
 }
 
+ElementsData *ElementsData::setElementsData(DEVICE_NAME device, dataKeeper &dk) {
+  return new ElementsData(device, dk);
+}
+
+void ElementOperator::getDiagonal(size_t, HostMatrix &diag) const {
+  dataKeeper &dk = ed_->keeper();
+  std::vector<double> d(dk.get_nodesCount() * dk.get_dim());
+  check(cfem_diagonal(dk.context(), d.data()), "getDiagonal");
+  HostMatrix m(dk.get_nodesCount(), dk.get_dim());
+  for (size_t i = 0; i < d.size(); ++i) m[i] = (float)d[i];
+  m.copy(diag);
+}
+
+void ElementsData::initFlocals(float t, const WaveletParams &w) {
+  cfem_wavelet cw = dk_.wavelet();
+  cw.type = w.waveletType == "ricker" ? CFEM_WAVELET_RICKER
+            : w.waveletType == "berlage" ? CFEM_WAVELET_BERLAGE : CFEM_WAVELET_NONE;
+  cw.freq = w.freq;
+  cw.timeshift = w.timeshift;
+  cw.ampl = w.ampl;
+  std::vector<double> f(dk_.get_nodesCount() * dk_.get_dim());
+  check(cfem_rhs(dk_.context(), &cw, (double)t, f.data()), "initFlocals");
+  HostMatrix m(dk_.get_nodesCount(), dk_.get_dim());
+  for (size_t i = 0; i < f.size(); ++i) m[i] = (float)f[i];
+  m.copy(Flocals_);
+}
+
+void gpuPCG_EbE_vec(HostMatrix &displacements, DEVICE_NAME deviceType, dataKeeper &FEMdata, ElementsData &elemsData,
+                    bool doAssemblyRes, float eps, bool PRINT_DEBUG_INFO) {
+  const size_t dim = FEMdata.get_dim(), nn = FEMdata.get_nodesCount(), nd = nn * dim;
+  HostMatrix *r = elemsData.get_r();
+  if (r->get_numElements() != nd)
+    throw Error(CFEM_ERR_INVALID_ARGUMENT, "gpuPCG_EbE_vec: elemsData.get_r() holds " +
+                                               std::to_string(r->get_numElements()) + " values, n_nodes * DIM is " +
+                                               std::to_string(nd) + " (initFlocals, then get_Flocals()->copy(*get_r()))");
+  std::vector<double> f(r->get_data(), r->get_data() + nd), u;
+  gpuPCG_EbE_vec(u, deviceType, FEMdata, f, eps, PRINT_DEBUG_INFO, nullptr);
+  if (doAssemblyRes) {
+    HostMatrix out(nn, dim);
+    for (size_t i = 0; i < nd; ++i) out[i] = (float)u[i];
+    out.copy(displacements);
+  } else {
+    const std::vector<int32_t> &el = FEMdata.get_elementsIds();
+    const size_t nv = dim + 1, ne = FEMdata.get_elementsCount(), w = nv * dim;
+    HostMatrix out(ne, w);
+    for (size_t e = 0; e < ne; ++e)
+      for (size_t a = 0; a < nv; ++a)
+        for (size_t d = 0; d < dim; ++d) out(e, a * dim + d) = (float)u[(size_t)el[e * nv + a] * dim + d];
+    out.copy(displacements);
+  }
+}
+
 void gpuCalculateFEM_DYN(DEVICE_NAME, dataKeeper &dk, bool PRINT_DEBUG_INFO, SolveReport *report) {
   cfem_ctx *c = dk.context();
   const MechanicalParams mp = dk.getMechParams();
@@ -489,6 +541,8 @@ void MakeVTKfile3D(const std::string &output_vtk, const std::vector<double> &nod
     out << std::sqrt(s) << "\n";
   }
 }
+
+void WriteResults(dataKeeper &dk, ResultsDataKeeper &) { WriteResults(dk); }
 
 void WriteResults(dataKeeper &dk) {
   const dataPaths p = dk.getDataPaths();

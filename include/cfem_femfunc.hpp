@@ -75,6 +75,12 @@ class HostMatrix {
   float operator()(size_t i, size_t j) const { return data_[j + i * cols_]; }
   float &operator[](size_t i) { return data_[i]; }
   void setTo(float v) { std::fill(data_.begin(), data_.end(), v); }
+  // Matrix::copy(Matrix &tgt) (matrix_pack_cpu.h): tgt takes this matrix's shape and values.
+  void copy(HostMatrix &tgt) const {
+    tgt.rows_ = rows_;
+    tgt.cols_ = cols_;
+    tgt.data_ = data_;
+  }
 
  private:
   size_t rows_ = 0, cols_ = 0;
@@ -140,16 +146,92 @@ struct SolveReport {
   cfem_dyn_info dyn_info{};
 };
 
+// datakeeper.h:200-226: the options and containers the reference's
+// WriteResults receives. The reference's WriteResults writes displacements
+// only and ignores them (femfunc.cpp:384-390); so does this one.
+class ResultsDataKeeper {
+ public:
+  ResultsDataKeeper(bool withStressAlongAxis, bool withSmooth, bool withMises, int nodesCount)
+      : withStressAlongAxis(withStressAlongAxis), withSmooth(withSmooth), withMises(withMises) {
+    (void)nodesCount;
+  }
+  bool withStressAlongAxis;
+  bool withSmooth;
+  bool withMises;
+  std::vector<HostMatrix> Deformation;
+  std::vector<HostMatrix> Stress;
+  std::vector<float> sigma_mises;
+  std::vector<float> epsilon_mises;
+  std::vector<float> StressComponents;
+  std::vector<float> MisesComponents;
+  std::vector<float> StressComponentsSmooth;
+  HostMatrix SmoothStress;
+};
+
+// The diagonal of the element operator as the reference reads it with
+// Klocals->getDiagonal(6 * (DIM - 1), diagK) (femfunc.cpp:10): here the
+// assembled diagonal of K' (n_nodes x DIM), which is what the reference's PCG
+// forms from it by assembly (femfunc.cpp:40).
+class ElementsData;
+class ElementOperator {
+ public:
+  explicit ElementOperator(ElementsData *ed) : ed_(ed) {}
+  void getDiagonal(size_t blockSize, HostMatrix &diag) const;
+
+ private:
+  ElementsData *ed_;
+};
+
+// fem_utils.h:24-148 (ElementsData), the calls a caller of gpuPCG_EbE_vec makes
+// (femfunc.cpp:3-23): the factory, genMask, calculateKlocals, getDiagonal,
+// initFlocals and the PCG vectors r and Flocals. The reference keeps those
+// vectors element-local (n_elems x 6(DIM-1), their assembly is the global
+// vector); this mirror keeps them assembled (n_nodes x DIM, caller node order),
+// which is the same right-hand side for the same solve. Like the reference's,
+// they are float. Mask, element matrices and geometry live in the GPU context
+// of the dataKeeper, built when it is first needed.
+class ElementsData {
+ public:
+  static ElementsData *setElementsData(DEVICE_NAME device, dataKeeper &dk);  // fem_utils.cpp:41-51
+  DEVICE_NAME get_device() const { return device_; }
+  void genMask() {}           // the DOF map is built with the context
+  void calculateKlocals() {}  // likewise the element operator (never stored as 12 x 12 matrices)
+  ElementOperator *get_Klocals() { return &klocals_; }
+  HostMatrix *get_diagK() { return &diagK_; }
+  // cpu_fem_utils.cpp:522-596 at time t with the run_config wavelet: the
+  // assembled right-hand side (tractions and point loads) into Flocals.
+  void initFlocals(float t, const WaveletParams &w);
+  HostMatrix *get_Flocals() { return &Flocals_; }
+  HostMatrix *get_r() { return &r_; }
+  dataKeeper &keeper() { return dk_; }
+
+ private:
+  ElementsData(DEVICE_NAME device, dataKeeper &dk) : device_(device), dk_(dk), klocals_(this) {}
+  DEVICE_NAME device_;
+  dataKeeper &dk_;
+  ElementOperator klocals_;
+  HostMatrix diagK_, Flocals_, r_;
+};
+
 // femfunc.cpp:3-23: static solve; result in dk.get_displacements().
 void gpuCalculateFEM_EbE_vec(DEVICE_NAME deviceType, dataKeeper &FEMdata, bool PRINT_DEBUG_INFO,
                              SolveReport *report = nullptr);
-// femfunc.cpp:25-128: Jacobi PCG for K' u = f with an explicit assembled
-// right-hand side f (n_nodes * DIM); eps as the reference's stopping factor.
+// femfunc.cpp:25-128 in the reference's argument order: Jacobi PCG for
+// K' u = r with the right-hand side the caller left in elemsData.get_r()
+// (femfunc.cpp:17: Flocals copied into r), stopping factor eps on
+// gamma = r.M^-1.r. doAssemblyRes true: displacements becomes n_nodes x DIM
+// (femfunc.cpp:100-105); false: the element-local copy x_e = u[mask_e],
+// n_elems x 6(DIM-1) (femfunc.cpp:107), as the reference's unassembled x.
+void gpuPCG_EbE_vec(HostMatrix &displacements, DEVICE_NAME deviceType, dataKeeper &FEMdata, ElementsData &elemsData,
+                    bool doAssemblyRes, float eps, bool PRINT_DEBUG_INFO);
+// The same solve for an FP64 right-hand side f (n_nodes * DIM) and an FP64
+// result; precision and stopping rule from the run_config "gb300" block.
 void gpuPCG_EbE_vec(std::vector<double> &displacements, DEVICE_NAME devType, dataKeeper &FEMdata,
                     const std::vector<double> &rhs, float eps, bool PRINT_DEBUG_INFO, SolveReport *report = nullptr);
 // femfunc.cpp:130-381: GN22 dynamics; result in dk.get_displacements().
 void gpuCalculateFEM_DYN(DEVICE_NAME devType, dataKeeper &dk, bool PRINT_DEBUG_INFO, SolveReport *report = nullptr);
 // femfunc.cpp:384-390 / VTKfile.cpp:281-386: legacy ASCII VTK at dk.getDataPaths().output_vtk.
+void WriteResults(dataKeeper &dk, ResultsDataKeeper &RESdata);
 void WriteResults(dataKeeper &dk);
 // The run_config "task" list (run_fem.py:16-18); a plain string is one task.
 std::vector<std::string> readTaskList(const std::string &configPath);

@@ -58,7 +58,17 @@ $(OUT)/obj/ref_driver.o: oracle/ref_driver.cpp
 $(OUT)/ref_driver: $(OBJS) $(OUT)/obj/ref_driver.o
 	$(CXX) -o $@ $(OUT)/obj/ref_driver.o -Wl,--start-group $(OBJS) -Wl,--end-group
 
+# the include list and the reference's objects, for callers that compile and
+# link their own code against the reference (tests/test_integration_branch.py)
+print-inc:
+	@echo $(INC)
+
+print-objs:
+	@echo $(OBJS)
+
+objs: $(OBJS)
+
 clean:
 	rm -rf $(OUT)
 
-.PHONY: all clean
+.PHONY: all clean print-inc print-objs objs

@@ -71,3 +71,69 @@ def test_cfem_run_executable(tmp_path):
         assert rel(meshio.read_vtk_displacements(str(vtk), 2), g) < 2e-5
     r = subprocess.run([build.EXE, str(tmp_path / "missing.json")], capture_output=True, text=True, timeout=60)
     assert r.returncode == 1 and "cannot open" in r.stderr
+
+
+CALLER = r"""
+// A caller written against the reference's interface (femfunc.h:20-24,
+// fem_utils.h ElementsData), compiled against include/cfem_femfunc.hpp: the
+// static flow of femfunc.cpp:3-23 with the reference's gpuPCG_EbE_vec
+// argument list, then WriteResults(dk, ResultsDataKeeper&).
+#include <cfem_femfunc.hpp>
+#include <cstdio>
+using namespace cfem_ref;
+int main(int argc, char **argv) {
+  dataKeeper dk(argv[1], argv[2]);
+  ElementsData *ed = ElementsData::setElementsData(GB300, dk);
+  ed->genMask();
+  ed->calculateKlocals();
+  ed->get_Klocals()->getDiagonal(6 * (dk.get_dim() - 1), *ed->get_diagK());
+  ed->initFlocals(0.f, dk.getWaveletParams());
+  ed->get_Flocals()->copy(*ed->get_r());
+  gpuPCG_EbE_vec(*dk.get_displacements(), GB300, dk, *ed, true, 1e-8f, false);
+  HostMatrix local;
+  gpuPCG_EbE_vec(local, GB300, dk, *ed, false, 1e-8f, false);
+  ResultsDataKeeper res(false, false, false, (int)dk.get_nodesCount());
+  WriteResults(dk, res);
+  FILE *f = std::fopen(argv[3], "wb");
+  std::fwrite(dk.get_displacements()->get_data(), 4, dk.get_displacements()->get_numElements(), f);
+  std::fwrite(local.get_data(), 4, local.get_numElements(), f);
+  std::fwrite(ed->get_diagK()->get_data(), 4, ed->get_diagK()->get_numElements(), f);
+  std::fclose(f);
+  std::printf("%zu %zu %zu\n", dk.get_displacements()->get_numElements(), local.get_numElements(),
+              ed->get_diagK()->get_numElements());
+  delete ed;
+  return 0;
+}
+"""
+
+
+@pytest.mark.parametrize("name,dim", [("test_rect_pcg", 2), ("box3", 3)])
+def test_reference_argument_lists_compile_and_solve(tmp_path, name, dim):
+    """gpuPCG_EbE_vec(Matrix&, DEVICE_NAME, dataKeeper&, ElementsData&, bool,
+    float, bool) and WriteResults(dataKeeper&, ResultsDataKeeper&) as the
+    reference declares them, from a compiled C++ caller: the assembled result,
+    the element-local result and the diagonal against the oracle."""
+    import cudafemproject_gb300 as pkg
+    pkg.lib()
+    libdir = os.path.join(os.path.dirname(pkg.__file__), "_lib")
+    inc = os.path.join(os.path.dirname(os.path.dirname(pkg.__file__)), "include")
+    src = tmp_path / "caller.cpp"
+    src.write_text(CALLER)
+    exe = str(tmp_path / "caller")
+    subprocess.run(["g++", "-O1", "-std=c++17", "-I", inc, str(src), "-o", exe, f"-L{libdir}", "-lcfem_gb300",
+                    f"-Wl,-rpath,{libdir}"], check=True, capture_output=True)
+    cfg = _work(tmp_path, dim, [name])
+    out = tmp_path / "out.bin"
+    r = subprocess.run([exe, cfg, name, str(out)], check=True, capture_output=True, text=True)
+    n_u, n_loc, n_d = (int(v) for v in r.stdout.split())
+    raw = np.fromfile(out, np.float32)
+    p = golden_problem(name, dim)
+    assert (n_u, n_loc, n_d) == (p.n_dof, p.n_elems * (dim + 1) * dim, p.n_dof)
+    u, loc, diag = raw[:n_u], raw[n_u:n_u + n_loc], raw[n_u + n_loc:]
+    o = O.Oracle(p)
+    x, _ = o.static(tol=1e-14, rule=1)
+    assert rel(u, x) < 1e-5  # FP32 PCG stopped by the reference's rule
+    # a second solve of the same system, gathered per element (x_e = u[mask_e])
+    assert rel(loc.reshape(p.n_elems, -1), u.reshape(-1, dim)[p.elems].reshape(p.n_elems, -1)) < 1e-6
+    assert rel(diag, o.diag()) < 1e-6
+    assert (tmp_path / "fem_results" / f"{dim}D" / name / "results.vtk").exists()
