@@ -524,15 +524,54 @@ void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, co
       for (int i = 0; i < n; ++i) cnt[i + 1] += cnt[i];
       const int total = cnt[n];
       for (int i = 0; i < c->L32.nps; ++i) fst[i] = (uint16_t)(i <= n ? cnt[i] : total);
-      for (int fl = 0; fl < nf; ++fl) {
-        const int len = P.fan_slot[(size_t)(f0 + fl) * kFanSlots + kFanSlots - 1];
-        for (int h = 0; h < 2; ++h)
-          for (int hs = 0; hs < half_slot_count(h, len); ++hs)
-            if (half_writes(h, hs)) {
-              const uint32_t pos = (uint32_t)cnt[P.fan_slot[(size_t)(f0 + fl) * kFanSlots + half_slot_to_fan(h, hs)]]++;
-              fp[(hs >> 1) * kHfanThreads + 2 * fl + h] |= pos << (16 * (hs & 1));
+      // Positions inside a node's run are free to choose (the node sum adds
+      // the whole run). The kernel stores slot hs of all half-threads of a warp
+      // with one 16-byte store instruction, served eight lanes (a quarter warp)
+      // per shared-memory wavefront when their addresses fall in different
+      // 16-byte bank groups (position mod 8; the force list starts 128-byte
+      // aligned). Positions are handed out per quarter warp and slot, the
+      // lanes with the fewest free positions first, each taking a free position
+      // of its node's run in a bank group no other lane of the quarter warp
+      // has taken where the run allows it.
+      std::vector<uint8_t> taken(total, 0);
+      for (int q0 = 0; q0 < 2 * nf; q0 += 8)
+        for (int hs = 0; hs < 6; ++hs) {
+          int lane_t[8], lane_node[8], m = 0;
+          for (int t = q0; t < q0 + 8 && t < 2 * nf; ++t) {
+            const int fl = t >> 1, h = t & 1;
+            const int len = P.fan_slot[(size_t)(f0 + fl) * kFanSlots + kFanSlots - 1];
+            if (hs < half_slot_count(h, len) && half_writes(h, hs)) {
+              lane_t[m] = t;
+              lane_node[m] = P.fan_slot[(size_t)(f0 + fl) * kFanSlots + half_slot_to_fan(h, hs)];
+              ++m;
             }
-      }
+          }
+          auto free_in_run = [&](int node) {
+            int k = 0;
+            for (int p = cnt[node]; p < cnt[node + 1]; ++p) k += !taken[p];
+            return k;
+          };
+          unsigned used = 0;
+          bool done[8] = {false, false, false, false, false, false, false, false};
+          for (int r = 0; r < m; ++r) {
+            int best = -1, best_free = 1 << 30;
+            for (int e = 0; e < m; ++e)
+              if (!done[e]) {
+                const int fr = free_in_run(lane_node[e]);
+                if (fr < best_free) best = e, best_free = fr;
+              }
+            const int node = lane_node[best];
+            int pos = -1;
+            for (int p = cnt[node]; p < cnt[node + 1] && pos < 0; ++p)
+              if (!taken[p] && !((used >> (p & 7)) & 1u)) pos = p;
+            for (int p = cnt[node]; p < cnt[node + 1] && pos < 0; ++p)
+              if (!taken[p]) pos = p;
+            taken[pos] = 1;
+            used |= 1u << (pos & 7);
+            done[best] = true;
+            fp[(hs >> 1) * kHfanThreads + lane_t[best]] |= (uint32_t)pos << (16 * (hs & 1));
+          }
+        }
       for (int i = 0; i < c->L32.npn; ++i) {
         nd[i] = i < n ? P.p_nodes[nb + i] : P.p_nodes[nb];
         bt[i] = i < n ? P.node_bits[P.p_nodes[nb + i]] : 0;

@@ -579,7 +579,9 @@ cfem_status cfem_set_young(cfem_ctx *ctx, const double *elem_young) {
     enter(ctx);
     if (!elem_young) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "null array"};
     std::vector<double> yv(ctx->ne);
-    CK(cudaMemcpy(yv.data(), elem_young, sizeof(double) * ctx->ne, cudaMemcpyDefault));
+    // on the context's stream, which enter() ordered after the caller's
+    CK(cudaMemcpyAsync(yv.data(), elem_young, sizeof(double) * ctx->ne, cudaMemcpyDefault, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
     for (double y : yv)
       if (!(y > 0)) throw Fail{CFEM_ERR_INVALID_ARGUMENT, "per-element Young's modulus must be positive"};
     ctx->young = yv;

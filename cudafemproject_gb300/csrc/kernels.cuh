@@ -463,11 +463,13 @@ __device__ __forceinline__ void element_force(const T (&u)[DIM + 1][DIM], const 
   }
 }
 
-// Stiffness action of a tet from vertex differences du_a = u_a - u_0 (a = 1..3):
-// forces on vertices 1..3 only (the force on vertex 0 is minus their sum).
+// Stiffness action of a tet from vertex differences du_a = u_a - u_0 (a = 1..3),
+// added to the forces f1..f3 on vertices 1..3 (the force on vertex 0 is minus
+// their sum): H = sum_a du_a (x) G_a, S = lam tr(H) I + mu (H + H^T),
+// f_a += S G_a, each component one fused multiply-add chain into f_a.
 // lam, mu already carry the operator's stiffness factor.
 template <typename T>
-__device__ __forceinline__ void tet_forces_rel(const T (&d1)[3], const T (&d2)[3], const T (&d3)[3], const T (&G)[9],
+__device__ __forceinline__ void tet_forces_acc(const T (&d1)[3], const T (&d2)[3], const T (&d3)[3], const T (&G)[9],
                                                T lam, T mu, T (&f1)[3], T (&f2)[3], T (&f3)[3]) {
   T H[3][3];
 #pragma unroll
@@ -484,9 +486,9 @@ __device__ __forceinline__ void tet_forces_rel(const T (&d1)[3], const T (&d2)[3
   S[1][2] = S[2][1] = mu * (H[1][2] + H[2][1]);
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    f1[i] = S[i][0] * G[0] + S[i][1] * G[1] + S[i][2] * G[2];
-    f2[i] = S[i][0] * G[3] + S[i][1] * G[4] + S[i][2] * G[5];
-    f3[i] = S[i][0] * G[6] + S[i][1] * G[7] + S[i][2] * G[8];
+    f1[i] = fma(S[i][2], G[2], fma(S[i][1], G[1], fma(S[i][0], G[0], f1[i])));
+    f2[i] = fma(S[i][2], G[5], fma(S[i][1], G[4], fma(S[i][0], G[3], f2[i])));
+    f3[i] = fma(S[i][2], G[8], fma(S[i][1], G[7], fma(S[i][0], G[6], f3[i])));
   }
 }
 

@@ -273,14 +273,7 @@ __global__ void __launch_bounds__(kHfanThreads, C <= 2 ? 3 : 2) k_matvec_multi(M
       for (int jj = 0; jj < 3; ++jj) {
         T G[9];
         load_tet_G(B + L.g_off, hf, jj, G);
-        T f1[3], f2[3], f3[3];
-        tet_forces_rel<T>(du[1], du[2 + jj], du[3 + jj], G, lam, mu, f1, f2, f3);
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) {
-          fv[1][d] += f1[d];
-          fv[2 + jj][d] += f2[d];
-          fv[3 + jj][d] += f3[d];
-        }
+        tet_forces_acc<T>(du[1], du[2 + jj], du[3 + jj], G, lam, mu, fv[1], fv[2 + jj], fv[3 + jj]);
       }
 #pragma unroll
       for (int d = 0; d < DIM; ++d) fv[0][d] = -(fv[1][d] + fv[2][d] + fv[3][d] + fv[4][d] + fv[5][d]);

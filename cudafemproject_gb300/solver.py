@@ -225,15 +225,23 @@ class FemContext:
 
     def adjoint(self, u, dLdu, precision="fp64", tol=1e-12, stop_rule="residual", max_iter=1000000, outer_tol=1e-13,
                 max_outer=50):
-        """lambda = K'^-1 dL/du; returns (dL/dE per element, dL/df = lambda, info)."""
-        u = np.ascontiguousarray(u, dtype=np.float64).ravel()
-        g = np.ascontiguousarray(dLdu, dtype=np.float64).ravel()
-        dE = np.zeros(self.n_elems, np.float64)
-        df = np.zeros(self.ndof, np.float64)
+        """lambda = K'^-1 dL/du; returns (dL/dE per element, dL/df = lambda, info).
+        With CUDA float64 tensors for u and dL/du the outputs are CUDA tensors
+        and nothing passes through the host."""
+        if hasattr(u, "data_ptr") and hasattr(dLdu, "data_ptr"):
+            import torch
+            u = u.contiguous().view(-1)
+            g = dLdu.contiguous().view(-1)
+            dE = torch.empty(self.n_elems, dtype=torch.float64, device=u.device)
+            df = torch.empty(self.ndof, dtype=torch.float64, device=u.device)
+        else:
+            u = np.ascontiguousarray(u, dtype=np.float64).ravel()
+            g = np.ascontiguousarray(dLdu, dtype=np.float64).ravel()
+            dE = np.zeros(self.n_elems, np.float64)
+            df = np.zeros(self.ndof, np.float64)
         prm = self._params(precision, tol, stop_rule, max_iter, outer_tol, max_outer)
         inf = capi.SolveInfo()
-        st = capi.lib().cfem_adjoint(self._h, C.byref(prm), u.ctypes.data, g.ctypes.data, dE.ctypes.data,
-                                     df.ctypes.data, C.byref(inf))
+        st = capi.lib().cfem_adjoint(self._h, C.byref(prm), _ptr(u), _ptr(g), _ptr(dE), _ptr(df), C.byref(inf))
         capi.check(st, "cfem_adjoint")
         return dE, df, self._info(inf)
 
@@ -263,8 +271,19 @@ class FemContext:
         return L.value, g, dict(steps=inf.steps, solve_ms=inf.solve_ms)
 
     def set_young(self, young):
-        y = np.ascontiguousarray(young, dtype=np.float64)
-        capi.check(capi.lib().cfem_set_young(self._h, y.ctypes.data), "cfem_set_young")
+        """Per-element Young's moduli [n_elems]: numpy, or a CUDA float64 tensor (read on the device)."""
+        y = young.contiguous() if hasattr(young, "data_ptr") else np.ascontiguousarray(young, dtype=np.float64)
+        capi.check(capi.lib().cfem_set_young(self._h, _ptr(y)), "cfem_set_young")
+
+    def set_stream(self, stream):
+        """Issue this context's work on ``stream`` (a cudaStream_t as an int, or
+        a torch.cuda.Stream); 0 / None: the legacy default stream, followed by a
+        stream of the context's own. Captured graphs are dropped on a change."""
+        s = getattr(stream, "cuda_stream", stream) or 0
+        if getattr(self, "_stream", 0) == s:
+            return
+        capi.check(capi.lib().cfem_set_stream(self._h, C.c_void_p(s) if s else None), "cfem_set_stream")
+        self._stream = s
 
     def dyn(self, beta1, beta2, dt, endtime, precision="fp64", wavelet: Optional[WaveletParams] = None,
             pcg_tol=1e-10, stop_rule="residual", max_iter=1000000, warm_start=True, receivers=None):

@@ -373,6 +373,58 @@ void orc_matvec(const orc_ctx *c, const double *x, double *y) {
   gsum(c, c->yloc, y);
 }
 
+/* Stress recovery per element (deprecated/femfunc/femfunc.cpp:42-106):
+ * strain = B u_e with the element's B (rows xx, yy, [zz,] xy, [yz, xz];
+ * engineering shear), stress = D strain with D scaled by E_e / E. The
+ * reference's von Mises line for 2D is commented out there; the textbook
+ * formula is used (2D: its commented expression; 3D: the usual invariant).
+ * The element B of the current reference divides the cofactors by |det|
+ * (cpu_fem_utils.cpp:396, 434), which is -grad N on an element of negative
+ * orientation: K_e = B'DB does not see the sign, a strain does. B is taken
+ * times sign(det) here, so that strain = sym(grad u) on every element. */
+void orc_element_stress(const orc_ctx *c, const double *u, double *strain, double *stress, double *mises) {
+  const int w = c->w, s = c->m.s;
+  const ebe_f64 *m = &c->m;
+#pragma omp parallel for schedule(static)
+  for (int64_t e = 0; e < c->ne; ++e) {
+    double eps[6] = {0, 0, 0, 0, 0, 0}, sig[6] = {0, 0, 0, 0, 0, 0};
+    const double *B = m->B + e * s * w;
+    const int nv = c->nv, dim = c->dim;
+    const double *x0 = m->nodes + (int64_t)m->el[e * nv] * dim;
+    double a[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    for (int k = 1; k < nv; ++k)
+      for (int d = 0; d < dim; ++d) a[k - 1][d] = m->nodes[(int64_t)m->el[e * nv + k] * dim + d] - x0[d];
+    const double det = dim == 2 ? a[0][0] * a[1][1] - a[0][1] * a[1][0]
+                                : a[0][0] * (a[1][1] * a[2][2] - a[1][2] * a[2][1]) -
+                                      a[0][1] * (a[1][0] * a[2][2] - a[1][2] * a[2][0]) +
+                                      a[0][2] * (a[1][0] * a[2][1] - a[1][1] * a[2][0]);
+    const double sgn = det < 0 ? -1.0 : 1.0;
+    for (int i = 0; i < s; ++i) {
+      for (int j = 0; j < w; ++j) eps[i] += B[i * w + j] * u[m->mask[e * w + j]];
+      eps[i] *= sgn;
+    }
+    const double sc = c->Ee[e] / c->E;
+    for (int i = 0; i < s; ++i) {
+      for (int k = 0; k < s; ++k) sig[i] += m->D[i + k * s] * eps[k];
+      sig[i] *= sc;
+    }
+    for (int i = 0; i < s; ++i) {
+      if (strain) strain[e * s + i] = eps[i];
+      if (stress) stress[e * s + i] = sig[i];
+    }
+    if (mises) {
+      double m2;
+      if (c->dim == 2)
+        m2 = sig[0] * sig[0] - sig[0] * sig[1] + sig[1] * sig[1] + 3 * sig[2] * sig[2];
+      else
+        m2 = 0.5 * ((sig[0] - sig[1]) * (sig[0] - sig[1]) + (sig[1] - sig[2]) * (sig[1] - sig[2]) +
+                    (sig[2] - sig[0]) * (sig[2] - sig[0])) +
+             3 * (sig[3] * sig[3] + sig[4] * sig[4] + sig[5] * sig[5]);
+      mises[e] = sqrt(m2);
+    }
+  }
+}
+
 /* Time factor applied to file loads in consistent mode. */
 static double consistent_scale(const orc_wavelet *wv, float t) {
   if (!wv || wv->type == ORC_WAVELET_NONE) return 1.0;

@@ -129,6 +129,10 @@ int orc_dyn_run(orc_ctx *c, const orc_wavelet *w, const orc_dyn *d, double pcg_t
  * Consistent semantics only. Returns L; g [n_elems]. */
 double orc_dyn_adjoint(orc_ctx *c, const orc_wavelet *w, const orc_dyn *d, int32_t n_rec, const int32_t *rec_nodes,
                        const double *obs, double *g);
+/* Per-element strain = B u_e, stress = D strain (D scaled by E_e / E) and
+ * von Mises stress (deprecated/femfunc/femfunc.cpp:42-106); outputs
+ * [n_elems][3(dim-1)] and [n_elems], any may be NULL. */
+void orc_element_stress(const orc_ctx *c, const double *u, double *strain, double *stress, double *mises);
 /* Adjoint sensitivity for a solved static state: dL/dE_e = -lambda_e^T (K_e / E_e) u_e. */
 void orc_grad_E(const orc_ctx *c, const double *lambda, const double *u, double *g);
 

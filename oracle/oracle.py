@@ -93,6 +93,7 @@ def lib():
         L.orc_dyn_run.argtypes = [C.c_void_p, W, D, C.c_double, C.c_int32, _f64p, C.POINTER(C.c_int32),
                                   C.POINTER(C.c_int64)]
         L.orc_grad_E.argtypes = [C.c_void_p, _f64p, _f64p, _f64p]
+        L.orc_element_stress.argtypes = [C.c_void_p, _f64p, _f64p, _f64p, _f64p]
         L.orc_dyn_adjoint.restype = C.c_double
         L.orc_dyn_adjoint.argtypes = [C.c_void_p, W, D, C.c_int32, _i32p, _f64p, _f64p]
         _lib = L
@@ -311,6 +312,15 @@ class Oracle:
         L = lib().orc_dyn_adjoint(self._h, C.byref(wavelet_struct(wavelet)), C.byref(d), len(rec), rec,
                                   np.ascontiguousarray(obs, np.float64).ravel(), g)
         return L, g
+
+    def element_stress(self, u):
+        """(strain, stress, von Mises) per element of displacements u."""
+        s = 3 * (self.p.dim - 1)
+        eps = np.zeros(self.p.n_elems * s)
+        sig = np.zeros(self.p.n_elems * s)
+        mis = np.zeros(self.p.n_elems)
+        lib().orc_element_stress(self._h, np.ascontiguousarray(u, np.float64).ravel(), eps, sig, mis)
+        return eps.reshape(-1, s), sig.reshape(-1, s), mis
 
     def grad_E(self, lam, u):
         g = np.zeros(self.p.n_elems, np.float64)

@@ -120,6 +120,38 @@ def test_torch_autograd_function():
     assert rel(f.grad.numpy(), lam) <= 1e-8
 
 
+@pytest.mark.parametrize("side_stream", [False, True])
+def test_torch_autograd_function_on_device(side_stream):
+    """CUDA tensors in, CUDA tensors out: the forward solve and the adjoint read
+    and write device memory only, on the caller's current torch stream (the
+    default one, or a side stream whose inputs were produced there)."""
+    torch = pytest.importorskip("torch")
+    from cudafemproject_gb300.autograd import static_solve
+    from cudafemproject_gb300.solver import FemContext
+    p = _problem(5)
+    ctx = FemContext(p, semantics="consistent")
+    f_host = ctx.rhs()
+    o = O.Oracle(p, consistent=True)
+    uo, _ = o.pcg(f_host, tol=1e-14, rule=1)
+    g = f_host.copy()
+    g[:30] += uo[:30]
+    lam, _ = o.pcg(g, tol=1e-14, rule=1)
+    s = torch.cuda.Stream() if side_stream else torch.cuda.current_stream()
+    with torch.cuda.stream(s):
+        # inputs made on this stream (a scaled copy, so their producer is a kernel there)
+        young = (torch.tensor(p.elem_E, dtype=torch.float64, device="cuda") * 1.0).requires_grad_(True)
+        f = (torch.tensor(f_host, dtype=torch.float64, device="cuda") * 1.0).requires_grad_(True)
+        u = static_solve(ctx, young, f, precision="fp64", tol=1e-13)
+        assert u.is_cuda
+        loss = (f.detach() * u).sum() + 0.5 * (u[:30] ** 2).sum()
+        loss.backward()
+    torch.cuda.synchronize()
+    assert young.grad.is_cuda and f.grad.is_cuda
+    assert rel(u.detach().cpu().numpy(), uo) <= 1e-10
+    assert rel(young.grad.cpu().numpy(), o.grad_E(lam, uo)) <= 1e-6
+    assert rel(f.grad.cpu().numpy(), lam) <= 1e-8
+
+
 def _dyn_problem(E):
     p = meshgen.box_3d(2, 2, 5, jitter=0.1, seed=1, rho=2000.0, traction=None,
                        point_load=("top_centre", (0.0, 0.0, -1e3)))

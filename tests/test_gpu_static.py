@@ -326,3 +326,37 @@ def test_pcg_termination_3d(precision):
     if precision == "fp64":
         x, _ = o.pcg(f, tol=1e-14, rule=1)
         assert rel(u, x) <= 1e-7
+
+
+@pytest.mark.parametrize("name,dim", [("box3", 3), ("box4p", 3), ("sq8", 2)])
+@pytest.mark.parametrize("consistent", [False, True])
+def test_element_stress_vs_oracle(name, dim, consistent):
+    """cfem_element_stress (strain, stress, von Mises per element) against the
+    oracle's restatement of the reference's recovery (strain = B u_e, stress =
+    D strain, deprecated/femfunc/femfunc.cpp:42-106) on the same displacement
+    field: the oracle's FP64 static solution of the task, compat and
+    consistent loads."""
+    from cudafemproject_gb300.solver import FemContext
+    p = golden_problem(name, dim)
+    o = O.Oracle(p, consistent=consistent)
+    u, _ = o.static(tol=1e-14, rule=1)
+    ctx = FemContext(p, semantics="consistent" if consistent else "compat")
+    eps, sig, mis = ctx.element_stress(u)
+    e_o, s_o, m_o = o.element_stress(u)
+    assert rel(eps, e_o) <= 1e-12
+    assert rel(sig, s_o) <= 1e-12
+    assert rel(mis, m_o) <= 1e-12
+
+
+def test_element_stress_delaunay_with_young_field():
+    """Unstructured tets of both orientations and per-element moduli."""
+    from cudafemproject_gb300.solver import FemContext
+    p = meshgen.random_tets(400, seed=3)
+    p.elem_E = 2e7 * np.exp(0.3 * np.random.default_rng(2).standard_normal(p.n_elems))
+    o = O.Oracle(p, consistent=True)
+    u = np.random.default_rng(5).standard_normal(p.n_dof) * 1e-3
+    eps, sig, mis = FemContext(p, semantics="consistent").element_stress(u)
+    e_o, s_o, m_o = o.element_stress(u)
+    assert rel(eps, e_o) <= 1e-12
+    assert rel(sig, s_o) <= 1e-12
+    assert rel(mis, m_o) <= 1e-12

@@ -144,3 +144,27 @@ def test_ebe_timer_runs_the_port_loop():
     assert t.iters(3) >= 0
     t.close()
     assert O.num_threads() >= 1
+
+
+@pytest.mark.parametrize("which", ["box", "square", "delaunay"])
+def test_oracle_stress_of_an_affine_field(which):
+    """strain = sym(grad u) exactly for u = A x on every element, whatever its
+    orientation (the Delaunay tets come in both), and stress = D strain."""
+    from cudafemproject_gb300 import meshgen
+    p = {"box": lambda: meshgen.box_3d(3, 3, 6, jitter=0.2, seed=1), "square": lambda: meshgen.square_2d(6),
+         "delaunay": lambda: meshgen.random_tets(300)}[which]()
+    d = p.dim
+    A = np.random.default_rng(0).standard_normal((d, d)) * 1e-3
+    eps, sig, mis = O.Oracle(p).element_stress((p.nodes @ A.T).ravel())
+    H = A
+    if d == 3:
+        exp = np.array([H[0, 0], H[1, 1], H[2, 2], H[0, 1] + H[1, 0], H[1, 2] + H[2, 1], H[0, 2] + H[2, 0]])
+        lam = p.E * p.nu / ((1 + p.nu) * (1 - 2 * p.nu))
+    else:
+        exp = np.array([H[0, 0], H[1, 1], H[0, 1] + H[1, 0]])
+        lam = p.E * p.nu / (1 - p.nu ** 2)  # plane stress
+    mu = p.E / (2 * (1 + p.nu))
+    assert np.abs(eps - exp).max() < 1e-11 * np.abs(exp).max()
+    tr = exp[:d].sum()
+    s_exp = np.concatenate([lam * tr + 2 * mu * exp[:d], mu * exp[d:]])
+    assert np.abs(sig - s_exp).max() < 1e-9 * np.abs(s_exp).max()
