@@ -493,8 +493,10 @@ def main():
         if err(u_dev.cpu().numpy()) <= TARGET_ERR:
             plain64 = kw
             break
+    # inner tolerances from 0.2 up continue the FP32 search direction across
+    # refinement steps (FP64 residual replacement); tighter ones restart
     refine, best = None, None
-    for inner in (1e-3, 1e-4):
+    for inner in (0.5, 0.4, 0.3, 0.25, 0.2, 1e-3):
         for outer in (1e-6, 1e-7, 1e-8, 1e-9, 1e-10):
             kw = dict(precision="fp32_refine", tol=inner, stop_rule="residual", outer_tol=outer, max_outer=30,
                       max_iter=40000)

@@ -151,7 +151,8 @@ void launch_update(cfem_ctx *c, const VecParams<T> &P) {
 // Jacobi PCG on A x = V.f with A = cM*M + cK*K' (mcoef selects the mass term).
 // V.x holds the warm start when warm != 0. Returns after the device flag says done.
 template <typename T>
-PcgResult run_pcg_t(cfem_ctx *c, Vecs<T> &V, T cK, T cM, const T *mcoef, int warm, double tol, int rule, int maxit) {
+PcgResult run_pcg_t(cfem_ctx *c, Vecs<T> &V, T cK, T cM, const T *mcoef, int warm, double tol, int rule, int maxit,
+                    const T *cont_p = nullptr, double cont_gamma_prev = 0) {
   Scalars *sc = c->sc.p + (sizeof(T) == 8 ? 0 : 1);
   Scalars h{};
   h.tol = tol;
@@ -171,6 +172,19 @@ PcgResult run_pcg_t(cfem_ctx *c, Vecs<T> &V, T cK, T cM, const T *mcoef, int war
     launch_mv<T>(c, MV_PLAIN, mv);
   }
   launch_init<T>(c, vec_params<T>(c, V, V.pA.p, sc), warm);
+  if (cont_p) {
+    // Continuation of an earlier run on a new residual: its last direction
+    // p_last stays, and the first direction becomes the conjugate-gradient
+    // step from it, z + (gamma / gamma_prev) p_last, folded into z here (the
+    // first matvec takes p = z).
+    CK(cudaMemcpyAsync(c->h_sc, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (!c->h_sc->done && cont_gamma_prev > 0) {
+      const T beta = (T)(c->h_sc->gamma / cont_gamma_prev);
+      k_add_scaled<T><<<nblk(c->nvec), kThreads, 0, c->stream>>>(c->nvec, beta, cont_p, V.z.p);
+      CKL();
+    }
+  }
   GraphCache &gc = sizeof(T) == 8 ? c->graph64 : c->graph32;
   if (!gc.exec || gc.key0 != (const void *)mcoef || gc.key1 != (double)cK || gc.key2 != (double)cM) {
     gc.reset();
@@ -230,6 +244,7 @@ PcgResult run_pcg_t(cfem_ctx *c, Vecs<T> &V, T cK, T cM, const T *mcoef, int war
   res.gamma = c->h_sc->gamma;
   res.rr = c->h_sc->rr;
   res.ff = c->h_sc->ff;
+  res.gamma_prev = c->h_sc->gamma_prev;
   int d = c->h_sc->done;
   res.status = d == 1 ? CFEM_OK : d == 2 ? CFEM_ERR_DIVERGED : CFEM_ERR_NOT_CONVERGED;
   return res;
@@ -304,6 +319,10 @@ void set_diag_vectors(cfem_ctx *c, const double *diagA64) {
   CKL();
 }
 
+// FP32_REFINE inner tolerances from which the inner PCG carries its search
+// direction across the refinement steps.
+constexpr double kContinueTol = 0.2;
+
 // Static-type solve of K' x = f (f internal FP64 in c->v64.f). Result in c->v64.x.
 cfem_status solve_internal(cfem_ctx *c, const cfem_solve_params *prm, cfem_solve_info *info) {
   cfem_solve_info inf{};
@@ -338,13 +357,32 @@ cfem_status solve_internal(cfem_ctx *c, const cfem_solve_params *prm, cfem_solve
     int outer = 0, total = 0;
     status = CFEM_ERR_NOT_CONVERGED;
     double rr_prev = -1;
+    int cont_iters = 0;  // iterations of the previous FP32 run (0: start the next one afresh)
+    double cont_gprev = 0;
+    const double stall = prm->tol >= kContinueTol ? std::min(0.9, std::max(0.25, 4.0 * prm->tol * prm->tol)) : 0.25;
     while (outer < max_outer) {
       if (std::sqrt(rr) <= outer_tol * std::sqrt(ff)) { status = CFEM_OK; break; }
       // The FP64 true residual has a floor near eps64 * ||K|| ||x||; once a
-      // refinement step no longer halves it the iterate is converged in FP64.
-      if (rr_prev >= 0 && rr > 0.25 * rr_prev) { status = CFEM_OK; break; }
+      // refinement step no longer reduces it as a step should (halves it; a
+      // continued step reduces it by about the replacement factor tol) the
+      // iterate is converged in FP64.
+      if (rr_prev >= 0 && rr > stall * rr_prev) { status = CFEM_OK; break; }
       rr_prev = rr;
-      PcgResult r = run_pcg<float>(c, c->v32, 1.f, 0.f, nullptr, 0, prm->tol, prm->stop_rule, prm->max_iter);
+      // With a loose inner tolerance (a residual-replacement factor, at least
+      // kContinueTol), from the second step on the FP32 PCG continues with its
+      // last direction (the step it ended on was taken with gamma_prev;
+      // iteration i writes its direction to pB when i is even, to pA when odd)
+      // instead of restarting from z: the FP64 true residual replaces the
+      // recursive one and the Krylov directions found so far keep serving.
+      // Replaced seldom, the recursive residual drifts too far from the true
+      // one for the old direction to stay conjugate, so tighter inner
+      // tolerances restart.
+      PcgResult r = cont_iters > 0 && prm->tol >= kContinueTol
+                        ? run_pcg_t<float>(c, c->v32, 1.f, 0.f, nullptr, 0, prm->tol, prm->stop_rule, prm->max_iter,
+                                           ((cont_iters - 1) & 1) ? c->v32.pA.p : c->v32.pB.p, cont_gprev)
+                        : run_pcg<float>(c, c->v32, 1.f, 0.f, nullptr, 0, prm->tol, prm->stop_rule, prm->max_iter);
+      cont_iters = r.status == CFEM_OK || r.status == CFEM_ERR_NOT_CONVERGED ? r.iters : 0;
+      cont_gprev = r.gamma_prev;
       total += r.iters;
       if (outer == 0) inf.gamma0 = r.gamma0;
       inf.gamma = r.gamma;

@@ -203,6 +203,7 @@ struct PcgResult {
   int status = CFEM_OK;
   int iters = 0;
   double gamma0 = 0, gamma = 0, rr = 0, ff = 0;
+  double gamma_prev = 0;  // the gamma of the last step length (alpha = gamma_prev / p.Ap)
 };
 
 MvParams<double> base_mv_d(cfem_ctx *c);

@@ -186,6 +186,13 @@ static __global__ void __launch_bounds__(kThreads) k_residual(ResParams P) {
   if (grid_sum_last<2>(acc, P.partials, P.count)) { P.out[0] = acc[0]; P.out[1] = acc[1]; }
 }
 
+// y += a x
+template <typename T>
+__global__ void k_add_scaled(int64_t n, T a, const T *x, T *y) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) y[i] += a * x[i];
+}
+
 // x64 += (double) x32
 static __global__ void k_accumulate(int64_t n, const float *x32, double *x64) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;

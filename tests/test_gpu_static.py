@@ -360,3 +360,21 @@ def test_element_stress_delaunay_with_young_field():
     assert rel(eps, e_o) <= 1e-12
     assert rel(sig, s_o) <= 1e-12
     assert rel(mis, m_o) <= 1e-12
+
+
+@pytest.mark.parametrize("inner", [0.2, 0.3, 0.5])
+@pytest.mark.parametrize("mesh", ["box", "delaunay"])
+def test_refinement_with_continued_directions(inner, mesh):
+    """FP32 + FP64 refinement with a loose inner tolerance (a residual
+    replacement factor from 0.2 up): the FP32 PCG keeps its search direction
+    across the FP64 true-residual replacements and still reaches the oracle's
+    solution to 1e-8."""
+    from cudafemproject_gb300.solver import FemContext
+    p = meshgen.box_3d(8, 8, 24, jitter=0.2, seed=5) if mesh == "box" else meshgen.random_tets(900, seed=4)
+    ctx = FemContext(p, semantics="consistent")
+    f = ctx.rhs()
+    x, _ = O.Oracle(p, consistent=True).pcg(f, tol=1e-14, rule=1)
+    u, info = ctx.pcg(f, "fp32_refine", tol=inner, stop_rule="residual", outer_tol=1e-10, max_outer=200)
+    assert info["status"] == 0
+    assert rel(u, x) <= 1e-8
+    assert info["outer_iterations"] > 1
