@@ -73,6 +73,7 @@ SIGNATURES = [
     ("cfem_create", i32, [C.POINTER(vp), C.POINTER(Mesh), C.POINTER(Material), C.POINTER(Options), vp]),
     ("cfem_destroy", None, [vp]),
     ("cfem_set_stream", i32, [vp, vp]),
+    ("cfem_selftest_copy_timeout", i32, [vp]),
     ("cfem_synchronize", i32, [vp]),
     ("cfem_get_counts", i32, [vp, vp]),
     ("cfem_dof_map", i32, [vp, vp]),

@@ -56,6 +56,8 @@ void launch_mv_t(cfem_ctx *c, int mode, const MvParams<T> &P) {
       F.fan_off = c->fan_off.p;
       F.fan_elem_off = c->fan_elem_off.p;
       F.err = c->tma_err.p;
+      F.skip_patch_plus1 = c->selftest_skip_plus1;
+      F.wait_limit = c->selftest_wait_limit;
       const double l2_half = 0.5 * c->l2_bytes;
       F.evict_first = (double)c->L32.bytes * c->prep.n_patches > l2_half;
       if (c->geo && !P.patch_inst) {
@@ -284,8 +286,9 @@ void to_internal_f(cfem_ctx *c, const double *src, float *dst, double scale) { t
 void to_caller_d(cfem_ctx *c, const double *src, double *dst) { to_caller_t<double>(c, src, dst); }
 void to_caller_f(cfem_ctx *c, const float *src, double *dst) { to_caller_t<float>(c, src, dst); }
 
-// FP64 true residual r = f - K' x (f, x internal FP64). Returns ||r||^2, ||f||^2.
-void true_residual(cfem_ctx *c, const double *f, const double *x, double *r, float *r32, double &rr, double &ff) {
+// FP64 true residual r = f - K' x (f, x internal FP64), ||r||^2 and ||f||^2
+// into the device doubles out2[0], out2[1]; queued on the context's stream.
+void true_residual_async(cfem_ctx *c, const double *f, const double *x, double *r, float *r32, double *out2) {
   MvParams<double> mv = base_mv<double>(c);
   mv.diagA = c->diagK.p;
   mv.x = x;
@@ -298,11 +301,16 @@ void true_residual(cfem_ctx *c, const double *f, const double *x, double *r, flo
   P.u = c->tmp64.p;
   P.r = r;
   P.r32 = r32;
-  P.out = c->rr.p;
+  P.out = out2;
   P.partials = c->partials.p;
   P.count = c->counters.p;
   k_residual<<<c->grid_vec, kThreads, 0, c->stream>>>(P);
   CKL();
+}
+
+// The same, waited for: returns ||r||^2, ||f||^2.
+void true_residual(cfem_ctx *c, const double *f, const double *x, double *r, float *r32, double &rr, double &ff) {
+  true_residual_async(c, f, x, r, r32, c->rr.p);
   CK(cudaMemcpyAsync(c->h_rr, c->rr.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   rr = c->h_rr[0];
@@ -318,10 +326,6 @@ void set_diag_vectors(cfem_ctx *c, const double *diagA64) {
   k_convert<double, float><<<nblk(c->nvec), kThreads, 0, c->stream>>>(c->nvec, diagA64, c->v32.diagA.p);
   CKL();
 }
-
-// FP32_REFINE inner tolerances from which the inner PCG carries its search
-// direction across the refinement steps.
-constexpr double kContinueTol = 0.2;
 
 // Static-type solve of K' x = f (f internal FP64 in c->v64.f). Result in c->v64.x.
 cfem_status solve_internal(cfem_ctx *c, const cfem_solve_params *prm, cfem_solve_info *info) {
@@ -359,7 +363,7 @@ cfem_status solve_internal(cfem_ctx *c, const cfem_solve_params *prm, cfem_solve
     double rr_prev = -1;
     int cont_iters = 0;  // iterations of the previous FP32 run (0: start the next one afresh)
     double cont_gprev = 0;
-    const double stall = prm->tol >= kContinueTol ? std::min(0.9, std::max(0.25, 4.0 * prm->tol * prm->tol)) : 0.25;
+    const double stall = refine_stall_ratio(prm->tol);
     while (outer < max_outer) {
       if (std::sqrt(rr) <= outer_tol * std::sqrt(ff)) { status = CFEM_OK; break; }
       // The FP64 true residual has a floor near eps64 * ||K|| ||x||; once a
@@ -1119,6 +1123,42 @@ cfem_status cfem_rhs(cfem_ctx *ctx, const cfem_wavelet *w, double t, double *f) 
     to_caller<double>(ctx, ctx->tmp64b.p, f);
     CK(cudaStreamSynchronize(ctx->stream));
     return CFEM_OK;
+  });
+}
+
+cfem_status cfem_selftest_copy_timeout(cfem_ctx *ctx) {
+  return run_guarded([&]() -> cfem_status {
+    check_ctx(ctx);
+    if (!(ctx->fans && ctx->fan_tma) || ctx->n_inst)
+      throw Fail{CFEM_ERR_UNSUPPORTED, "the copy-timeout self-test needs a single-mesh 3D edge-fan context"};
+    enter(ctx);
+    // one FP32 matvec whose first block of patch 0 is never requested, with
+    // the waits bounded at ~1 ms: CTA 0 must give up, flag the failure and
+    // return, and the host must report it
+    MvParams<float> mv = base_mv<float>(ctx);
+    mv.diagA = ctx->v32.diagA.p;
+    mv.x = ctx->v32.z.p;
+    mv.y = ctx->v32.u.p;
+    ctx->v32.z.zero(ctx->stream);
+    ctx->v32.u.zero(ctx->stream);
+    ctx->selftest_skip_plus1 = 1;
+    ctx->selftest_wait_limit = 2000000;
+    try {
+      launch_mv<float>(ctx, MV_PLAIN, mv);
+    } catch (...) {
+      ctx->selftest_skip_plus1 = 0;
+      ctx->selftest_wait_limit = 0;
+      throw;
+    }
+    ctx->selftest_skip_plus1 = 0;
+    ctx->selftest_wait_limit = 0;
+    try {
+      check_copy_error(ctx);
+    } catch (const Fail &f) {
+      if (f.st == CFEM_ERR_CUDA) return CFEM_OK;  // detected, reported and cleared
+      throw;
+    }
+    throw Fail{CFEM_ERR_CUDA, "self-test: a withheld bulk copy was not reported"};
   });
 }
 

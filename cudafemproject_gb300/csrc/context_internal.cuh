@@ -132,6 +132,8 @@ struct cfem_ctx {
   DBuf<int32_t> fan_patch;
   DBuf<int> tma_err;
   int *h_tma_err = nullptr;
+  int selftest_skip_plus1 = 0;       // FanTmaParams::skip_patch_plus1 (cfem_selftest_copy_timeout only)
+  long long selftest_wait_limit = 0;  // FanTmaParams::wait_limit (likewise)
   size_t smem_ft32 = 0;
   int grid_ft32 = 0;
   // geometry blocks (FP32 single-RHS matvec of CFEM_FORM_GEOMETRY_FAN): the
@@ -199,6 +201,17 @@ struct cfem_ctx {
 namespace cfem {
 namespace detail {
 
+// FP32_REFINE inner tolerances from which the inner PCG carries its search
+// direction across the refinement steps (the tolerance is then the factor by
+// which its recursive residual drops between FP64 true-residual replacements).
+constexpr double kContinueTol = 0.2;
+// A refinement step whose FP64 residual norm^2 falls by less than this is at
+// the FP64 floor: a restarted step halves the norm at least, a continued one
+// cuts it by about the replacement factor.
+inline double refine_stall_ratio(double tol) {
+  return tol >= kContinueTol ? std::min(0.9, std::max(0.25, 4.0 * tol * tol)) : 0.25;
+}
+
 struct PcgResult {
   int status = CFEM_OK;
   int iters = 0;
@@ -220,6 +233,7 @@ void to_caller_d(cfem_ctx *c, const double *src, double *dst);
 void to_caller_f(cfem_ctx *c, const float *src, double *dst);
 void set_diag_vectors(cfem_ctx *c, const double *diagA64);
 void true_residual(cfem_ctx *c, const double *f, const double *x, double *r, float *r32, double &rr, double &ff);
+void true_residual_async(cfem_ctx *c, const double *f, const double *x, double *r, float *r32, double *out2);
 void make_rhs(cfem_ctx *c, double a, double b, double *dst);
 cfem_status run_guarded(const std::function<cfem_status()> &fn);
 void check_ctx(const cfem_ctx *c);

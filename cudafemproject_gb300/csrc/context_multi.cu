@@ -25,6 +25,9 @@ struct MultiState {
   DBuf<double> partials, gpart;
   DBuf<unsigned> gcnt;  // group tickets: [0, n) matvec, [n, 2n) vector kernel
   DBuf<int> active;
+  DBuf<double> res_norms;  // [K][2] ||r_c||^2, ||f_c||^2 of the FP64 true residuals
+  DBuf<float> fold_beta;  // [K] continuation of the next run: z_c += beta_c p_last_c
+  DBuf<int> fold_par;     // [K] p_last_c in pA (1) or pB (0)
   MultiCtl *h_ctl = nullptr;
   std::vector<MultiScalars> h_sc;
   int grid_mv = 0, grid_vec = 0;
@@ -161,6 +164,9 @@ MultiState &multi_state(cfem_ctx *c, int K) {
   M->ctl.alloc(1);
   M->ctl.zero(c->stream);
   M->active.alloc(K);
+  M->res_norms.alloc((size_t)2 * K);
+  M->fold_beta.alloc(K);
+  M->fold_par.alloc(K);
   CK(cudaMallocHost(&M->h_ctl, sizeof(MultiCtl)));
   M->h_sc.resize(K);
   // four items per thread per round: two CTAs per SM keep enough loads in flight
@@ -183,9 +189,19 @@ void launch_vec(cfem_ctx *c, MultiState &M, const MultiParams<float> &P, const f
   c->launches += 1;
 }
 
+// Continuation of a multi-RHS run: per case the last run's iteration count (0:
+// start afresh) and the gamma of its last step length.
+struct MultiCont {
+  std::vector<int> iters;
+  std::vector<double> gamma_prev;
+};
+
 // Multi-RHS FP32 PCG on M.f (cases >= k_active are padding). Returns after
-// every case has stopped; per-case results in M.h_sc.
-void run_pcg_multi(cfem_ctx *c, MultiState &M, int k_active, double tol, int rule, int maxit) {
+// every case has stopped; per-case results in M.h_sc. With `cont`, cases with
+// a previous run start from the conjugate-gradient step off its last direction
+// (z_c + gamma_c / gamma_prev_c p_last_c), as run_pcg_t does for one case.
+void run_pcg_multi(cfem_ctx *c, MultiState &M, int k_active, double tol, int rule, int maxit,
+                   const MultiCont *cont = nullptr) {
   MultiCtl h{};
   h.tol = tol;
   h.rule = rule;
@@ -195,6 +211,28 @@ void run_pcg_multi(cfem_ctx *c, MultiState &M, int k_active, double tol, int rul
   M.gcnt.zero(c->stream);  // (tickets of a launch that stopped early are not left behind)
   MultiParams<float> P = multi_params(c, M);
   launch_vec(c, M, P, nullptr, 1);
+  if (cont) {
+    CK(cudaMemcpyAsync(M.h_sc.data(), M.sc.p, sizeof(MultiScalars) * M.K, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    std::vector<float> beta(M.K, 0.f);
+    std::vector<int> par(M.K, 0);
+    bool any = false;
+    for (int cs = 0; cs < M.K && cs < (int)cont->iters.size(); ++cs) {
+      if (M.h_sc[cs].done || cont->iters[cs] <= 0 || !(cont->gamma_prev[cs] > 0)) continue;
+      beta[cs] = (float)(M.h_sc[cs].gamma / cont->gamma_prev[cs]);
+      par[cs] = (cont->iters[cs] - 1) & 1;
+      any = true;
+    }
+    if (any) {
+      CK(cudaMemcpyAsync(M.fold_beta.p, beta.data(), sizeof(float) * M.K, cudaMemcpyHostToDevice, c->stream));
+      CK(cudaMemcpyAsync(M.fold_par.p, par.data(), sizeof(int) * M.K, cudaMemcpyHostToDevice, c->stream));
+      const int64_t items = (int64_t)c->nn * M.K;
+      k_multi_fold<<<nblk(items), kThreads, 0, c->stream>>>(items, M.K, M.fold_beta.p, M.fold_par.p, M.pA.p, M.pB.p,
+                                                            M.z.p);
+      CKL();
+      CK(cudaStreamSynchronize(c->stream));  // (beta and par are pageable)
+    }
+  }
   if (!M.graph) {
     cudaGraph_t graph;
     const int64_t before = c->launches;
@@ -272,15 +310,30 @@ cfem_status solve_batch(cfem_ctx *c, const cfem_solve_params &p, int kb, const d
   CK(cudaEventRecord(c->ev0, c->stream));
   std::vector<int> iters(kb, 0), outer(kb, 0), status(kb, CFEM_ERR_NOT_CONVERGED);
   std::vector<double> gamma0(kb, 0), gamma(kb, 0), rr(kb, 0), ff(kb, 0), rr_prev(kb, -1);
-  auto residuals = [&]() {
-    // r_c = f_c - K' x_c in FP64, case by case, with ||r_c||^2 and ||f_c||^2
+  std::vector<double> norms(2 * (size_t)kb, 0.0);
+  auto residuals = [&](bool all) {
+    // r_c = f_c - K' x_c in FP64 with ||r_c||^2 and ||f_c||^2 for the cases
+    // still running (all: every case), all queued on the stream and read back once
+    auto wanted = [&](int cs) { return all || (status[cs] != CFEM_OK && status[cs] != CFEM_ERR_DIVERGED); };
+    int queued = 0;
     for (int cs = 0; cs < kb; ++cs) {
+      if (!wanted(cs)) continue;
       k_case_copy<double, double><<<nblk(nn), kThreads, 0, c->stream>>>(nn, K, cs, M.f64.p, M.s_f.p, 1);
       k_case_copy<double, double><<<nblk(nn), kThreads, 0, c->stream>>>(nn, K, cs, M.x64.p, M.s_x.p, 1);
       CKL();
-      true_residual(c, M.s_f.p, M.s_x.p, M.s_r.p, nullptr, rr[cs], ff[cs]);
+      true_residual_async(c, M.s_f.p, M.s_x.p, M.s_r.p, nullptr, M.res_norms.p + 2 * cs);
       k_case_copy<double, double><<<nblk(nn), kThreads, 0, c->stream>>>(nn, K, cs, M.s_r.p, M.r64.p, 0);
       CKL();
+      ++queued;
+    }
+    if (!queued) return;
+    CK(cudaMemcpyAsync(norms.data(), M.res_norms.p, sizeof(double) * 2 * kb, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    check_copy_error(c);
+    for (int cs = 0; cs < kb; ++cs) {
+      if (!wanted(cs)) continue;
+      rr[cs] = norms[2 * cs];
+      ff[cs] = norms[2 * cs + 1];
     }
   };
   if (p.precision == CFEM_FP32) {
@@ -298,9 +351,13 @@ cfem_status solve_batch(cfem_ctx *c, const cfem_solve_params &p, int kb, const d
   } else {  // FP32 inner PCG in FP64 iterative refinement, per-case outer tests
     M.x64.zero(c->stream);
     CK(cudaMemcpyAsync(M.r64.p, M.f64.p, sizeof(double) * nitems * 4, cudaMemcpyDeviceToDevice, c->stream));
-    residuals();
+    residuals(false);
     const double outer_tol = p.outer_tol > 0 ? p.outer_tol : 1e-12;
     const int max_outer = p.max_outer > 0 ? p.max_outer : 50;
+    const double stall = refine_stall_ratio(p.tol);
+    // loose inner tolerances: every case continues its last direction (see solve_internal)
+    MultiCont cont{std::vector<int>(K, 0), std::vector<double>(K, 0.0)};
+    const bool continued = p.tol >= kContinueTol;
     std::vector<int> act(K, 0);
     for (int round = 0; round <= max_outer; ++round) {
       int n_act = 0;
@@ -310,7 +367,7 @@ cfem_status solve_batch(cfem_ctx *c, const cfem_solve_params &p, int kb, const d
         const bool conv = std::sqrt(rr[cs]) <= outer_tol * std::sqrt(ff[cs]);
         // the FP64 true residual has a floor near eps64 * ||K|| ||x||: a
         // refinement step that no longer halves it ends the case
-        const bool stalled = rr_prev[cs] >= 0 && rr[cs] > 0.25 * rr_prev[cs];
+        const bool stalled = rr_prev[cs] >= 0 && rr[cs] > stall * rr_prev[cs];
         if (conv || stalled || ff[cs] == 0.0) { status[cs] = CFEM_OK; continue; }
         if (round == max_outer) continue;
         act[cs] = 1;
@@ -320,9 +377,12 @@ cfem_status solve_batch(cfem_ctx *c, const cfem_solve_params &p, int kb, const d
       CK(cudaMemcpyAsync(M.active.p, act.data(), sizeof(int) * K, cudaMemcpyHostToDevice, c->stream));
       k_multi_cast_active<<<nblk(nitems), kThreads, 0, c->stream>>>(nn, K, M.r64.p, M.active.p, M.f.p);
       CKL();
-      run_pcg_multi(c, M, kb, p.tol, p.stop_rule, p.max_iter);
+      run_pcg_multi(c, M, kb, p.tol, p.stop_rule, p.max_iter, continued ? &cont : nullptr);
       for (int cs = 0; cs < kb; ++cs) {
         if (!act[cs]) continue;
+        const int d = M.h_sc[cs].done;
+        cont.iters[cs] = d == 1 || d == 3 ? M.h_sc[cs].iters : 0;
+        cont.gamma_prev[cs] = M.h_sc[cs].gamma_prev;
         iters[cs] += M.h_sc[cs].iters;
         if (outer[cs] == 0) gamma0[cs] = M.h_sc[cs].gamma0;
         gamma[cs] = M.h_sc[cs].gamma;
@@ -332,14 +392,14 @@ cfem_status solve_batch(cfem_ctx *c, const cfem_solve_params &p, int kb, const d
       }
       k_multi_accumulate<<<nblk(nitems * 4), kThreads, 0, c->stream>>>(nitems * 4, M.x.p, M.x64.p);
       CKL();
-      residuals();
+      residuals(false);
     }
   }
   CK(cudaEventRecord(c->ev1, c->stream));
   CK(cudaEventSynchronize(c->ev1));
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
-  if (p.precision == CFEM_FP32) residuals();  // relative residuals for the report
+  if (p.precision == CFEM_FP32) residuals(true);  // relative residuals for the report
   k_multi_to_caller<double><<<nblk(nitems), kThreads, 0, c->stream>>>(nn, K, kb, c->nd, M.x64.p, c->node_new2old.p,
                                                                         M.io.p);
   CKL();

@@ -189,6 +189,11 @@ struct FanTmaParams {
   int *err;                     // kErrTmaTimeout on a copy that never completed
   int evict_first;              // blocks larger than about half the L2: stream them with an
                                 // evict-first policy, so that the node vectors stay resident
+  // Self-test of the copy-timeout path (cfem_selftest_copy_timeout), zero
+  // otherwise: the first copy of patch skip_patch_plus1 - 1 is never issued,
+  // and the waits give up after wait_limit cycles.
+  int skip_patch_plus1;
+  long long wait_limit;
 };
 
 template <typename T, int MODE, bool GEO = false>
@@ -210,6 +215,7 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
   constexpr bool PREFETCH = GEO && MODE == MV_PCG;
   const int stage_stride = 2 * L.npn * VW;
   const bool batch = P.patch_inst != nullptr;
+  const long long lim = F.wait_limit > 0 ? F.wait_limit : kWaitCycles;
   T lam = P.lam, mu = P.mu;
   __shared__ unsigned warps_done[2];  // warps finished with buffer 0 / 1 (see the end of the patch loop)
   if (threadIdx.x == 0) {
@@ -244,7 +250,8 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
   // kernel wrote.
   if (threadIdx.x == 0 && !batch)
     for (int k = 0; k < 2; ++k)
-      if (blockIdx.x + k * step < P.n_patches) issue_copy(blockIdx.x + k * step, k);
+      if (blockIdx.x + k * step < P.n_patches && blockIdx.x + k * step != F.skip_patch_plus1 - 1)
+        issue_copy(blockIdx.x + k * step, k);
   griddep_wait();
   // single mesh: beta and the stopping test from the update's partials (every
   // CTA alike; the staging area, not in use yet, is the reduction scratch).
@@ -258,7 +265,7 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
   if (stopped) {
     if (threadIdx.x == 0 && !batch)  // let the copies issued above land before the CTA exits
       for (int k = 0; k < 2; ++k)
-        if (blockIdx.x + k * step < P.n_patches) mbar_wait_bounded(&bar[k], 0u);
+        if (blockIdx.x + k * step < P.n_patches) mbar_wait_bounded(&bar[k], 0u, lim);
     return;
   }
   if (batch && MODE == MV_PCG) {
@@ -281,7 +288,7 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
     }
   };
   if constexpr (PREFETCH) {
-    if (blockIdx.x < P.n_patches && mbar_wait_bounded(&bar[0], 0u)) issue_gathers(buf0, sp);
+    if (blockIdx.x < P.n_patches && mbar_wait_bounded(&bar[0], 0u, lim)) issue_gathers(buf0, sp);
     cp_async_commit();
   }
   DotAcc<T> energy;
@@ -295,7 +302,7 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
     const bool live = patch_live(patch);
     bool ok = true;
     if (live) {
-      ok = mbar_wait_bounded(&bar[b], (phase >> b) & 1u);
+      ok = mbar_wait_bounded(&bar[b], (phase >> b) & 1u, lim);
       phase ^= 1u << b;
     }
     auto copy_failed = [&]() {
@@ -303,7 +310,7 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
       if (threadIdx.x == 0) {
         atomicOr(F.err, kErrTmaTimeout);
         if (patch + step < P.n_patches && patch_live(patch + step))
-          mbar_wait_bounded(&bar[b ^ 1], (phase >> (b ^ 1)) & 1u);
+          mbar_wait_bounded(&bar[b ^ 1], (phase >> (b ^ 1)) & 1u, lim);
       }
     };
     if (batch && __syncthreads_or(!ok)) {  // (uniform: batch is a kernel parameter)
@@ -375,8 +382,8 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
       stage_load(i0, true);
       if (pcg_matvec_scalars<T>(P.sc, P.up_part, P.n_up, beta, red_pcg)) {
         if (threadIdx.x == 0) {  // the copies issued above land before the CTA exits
-          if (!ok) mbar_wait_bounded(&bar[b], 0u);
-          if (patch + step < P.n_patches) mbar_wait_bounded(&bar[b ^ 1], (phase >> (b ^ 1)) & 1u);
+          if (!ok) mbar_wait_bounded(&bar[b], 0u, lim);
+          if (patch + step < P.n_patches) mbar_wait_bounded(&bar[b ^ 1], (phase >> (b ^ 1)) & 1u, lim);
         }
         return;
       }
@@ -526,7 +533,7 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
         stv<T, VW>(fs, half_fpos(B + L.fpos_off, threadIdx.x, k), o);
       }
     if constexpr (PREFETCH) {  // the next patch's gathers overlap the node sums below
-      if (patch + step < P.n_patches && mbar_wait_bounded(&bar[b ^ 1], (phase >> (b ^ 1)) & 1u))
+      if (patch + step < P.n_patches && mbar_wait_bounded(&bar[b ^ 1], (phase >> (b ^ 1)) & 1u, lim))
         issue_gathers(b ? buf0 : buf1, sp + (size_t)((it + 1) & 1) * stage_stride);
       cp_async_commit();
     }

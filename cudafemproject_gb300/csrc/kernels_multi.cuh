@@ -211,6 +211,7 @@ __global__ void __launch_bounds__(kHfanThreads, C <= 2 ? 3 : 2) k_matvec_multi(M
     const int nn = hdr[0], own = hdr[1];
     const int n_it = nn * C;  // staging / output items (node i, case cl): it = i * C + cl
     const T beta = MODE == MV_PCG ? s_beta[c0 + cl] : T(0);
+    const bool case_done = MODE == MV_PCG && s_done[c0 + cl] != 0;
     // 1. stage the chunk's node values: C cases of a node are one contiguous load
     for (int i0 = threadIdx.x; i0 < n_it; i0 += SU * kHfanThreads) {
       NodeV<T, VW> v[SU], w[SU];
@@ -234,7 +235,9 @@ __global__ void __launch_bounds__(kHfanThreads, C <= 2 ? 3 : 2) k_matvec_multi(M
 #pragma unroll
             for (int d = 0; d < DIM; ++d) v[u].v[d] += beta * w[u].v[d];
           }
-          if (i >= own) stv<T, VW>(pnew, (int64_t)gi[u] * K + c0 + cl, v[u]);
+          // a stopped case keeps its last direction (a continued refinement
+          // step starts from it); its lanes still compute, unused
+          if (i >= own && !case_done) stv<T, VW>(pnew, (int64_t)gi[u] * K + c0 + cl, v[u]);
         }
         const unsigned bb = bits[i];
         NodeV<T, VW> m;
@@ -359,6 +362,23 @@ __global__ void __launch_bounds__(kHfanThreads, C <= 2 ? 3 : 2) k_matvec_multi(M
     s.sigma = t;
     s.alpha = s.done ? 0.0 : s.gamma / t;
   }
+}
+
+// z_c += beta_c p_c for every (node, case) item, p_c read from pB when
+// parity_c is 0, from pA when 1 (cases with beta_c = 0 are left alone): the
+// first direction of a continued multi-RHS run.
+static __global__ void k_multi_fold(int64_t n_items, int K, const float *beta, const int *parity, const float *pA,
+                                    const float *pB, float *z) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= n_items) return;
+  const int c = (int)(q % K);
+  const float b = beta[c];
+  if (b == 0.f) return;
+  const NodeV<float, 4> p = ldv<float, 4>(parity[c] ? pA : pB, q);
+  NodeV<float, 4> v = ldv<float, 4>(z, q);
+#pragma unroll
+  for (int d = 0; d < 3; ++d) v.v[d] += b * p.v[d];
+  stv<float, 4>(z, q, v);
 }
 
 // Per case: init (r = f, x = 0) or update (x += alpha p, r -= alpha u),

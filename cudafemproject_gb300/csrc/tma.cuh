@@ -77,12 +77,14 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
   return ok != 0;
 }
 
-// Waits for the mbarrier phase with the given parity; false after about one
-// second of clock64 time (the copy never completed).
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity) {
+constexpr long long kWaitCycles = 2000000000LL;  // about one second of clock64 time
+
+// Waits for the mbarrier phase with the given parity; false after `limit`
+// clock64 cycles (the copy never completed).
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity, long long limit = kWaitCycles) {
   const long long t0 = clock64();
   while (!mbar_try_wait(bar, parity))
-    if (clock64() - t0 > 2000000000LL) return false;
+    if (clock64() - t0 > limit) return false;
   return true;
 }
 

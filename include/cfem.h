@@ -318,6 +318,16 @@ CFEM_API cfem_status cfem_dyn_adjoint(cfem_ctx *ctx, const cfem_dyn_params *prm,
  * counterpart in the reference. */
 #define CFEM_NOALLOC_MAX_BLOCKS 4096
 CFEM_API cfem_status cfem_matvec_energy_noalloc(cfem_ctx *ctx, const double *x, double *y, double *energy);
+/* Self-test of the failure path of the FP32 edge-fan matvec's bulk copies
+ * (3D single-mesh contexts): runs one matvec in which the first block of patch
+ * 0 is never requested and the copy waits give up after ~1 ms, and checks
+ * that the kernel flags the missing copy, returns, and the host reports it as
+ * CFEM_ERR_CUDA ("a bulk copy ... did not complete in time"). Returns CFEM_OK
+ * when all of that happened; the context stays usable. No GPU fault is
+ * involved: the waits are bounded and nothing is read from the missing
+ * block. Has no counterpart in the reference (its GPU path has no bulk
+ * copies). */
+CFEM_API cfem_status cfem_selftest_copy_timeout(cfem_ctx *ctx);
 /* Per-element Young's modulus update (keeps geometry; rebuilds operator scale). */
 CFEM_API cfem_status cfem_set_young(cfem_ctx *ctx, const double *elem_young);
 

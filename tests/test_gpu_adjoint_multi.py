@@ -226,3 +226,26 @@ def test_multi_rhs_each_item_width(cases_per_item, monkeypatch):
     U32, _ = ctx.pcg_multi(F, precision="fp32", tol=1e-6, stop_rule="residual")
     for i, x in xs.items():
         assert rel(U32[i], x) <= 1e-4, i
+
+
+@pytest.mark.parametrize("cases_per_item", [2, 4, 8])
+def test_multi_rhs_continued_refinement(cases_per_item, monkeypatch):
+    """Multi-RHS FP32 + refinement with a loose inner tolerance (0.3): each
+    case continues its last search direction across the FP64 true-residual
+    replacements (stopped cases keep theirs), and every case still reaches the
+    FP64 oracle's solution to 1e-8; one zero case stays zero."""
+    from cudafemproject_gb300.solver import FemContext
+    monkeypatch.setenv("CFEM_MULTI_CASES", str(cases_per_item))
+    p = meshgen.box_3d(6, 6, 20, jitter=0.2, seed=12)
+    o = O.Oracle(p)
+    rng = np.random.default_rng(23)
+    F = rng.standard_normal((13, p.n_dof)) * 10.0 ** rng.uniform(2, 4, size=(13, 1))
+    F[4] = 0.0
+    ctx = FemContext(p)
+    U, infos = ctx.pcg_multi(F, precision="fp32_refine", tol=0.3, stop_rule="residual", outer_tol=1e-11,
+                             max_outer=200)
+    assert np.all(U[4] == 0.0)
+    for i in (0, 7, 12):
+        x, _ = o.pcg(F[i], tol=1e-14, rule=1)
+        assert rel(U[i], x) <= 1e-8, i
+        assert infos[i]["status"] == 0 and infos[i]["outer_iterations"] > 1

@@ -378,3 +378,25 @@ def test_refinement_with_continued_directions(inner, mesh):
     assert info["status"] == 0
     assert rel(u, x) <= 1e-8
     assert info["outer_iterations"] > 1
+
+
+def test_copy_timeout_is_reported_and_context_recovers():
+    """The failure path of the FP32 matvec's bulk copies, without a fault: a
+    matvec whose first block of patch 0 is never requested, with the copy
+    waits bounded at ~1 ms (cfem_selftest_copy_timeout). The kernel must give
+    up, flag the missing copy and return, the host must report it, and the
+    same context must then solve normally."""
+    from cudafemproject_gb300 import capi
+    from cudafemproject_gb300.solver import FemContext
+    p = meshgen.box_3d(6, 6, 18, jitter=0.2, seed=2)
+    ctx = FemContext(p, semantics="consistent")
+    assert ctx.counts()["matvec_form"] == capi.FORM_GRADIENT_FAN
+    L = capi.lib()
+    for _ in range(2):
+        assert L.cfem_selftest_copy_timeout(ctx._h) == capi.OK, L.cfem_last_error_string()
+    f = ctx.rhs()
+    x, _ = O.Oracle(p, consistent=True).pcg(f, tol=1e-14, rule=1)
+    u, info = ctx.pcg(f, "fp32_refine", tol=1e-4, stop_rule="residual", outer_tol=1e-12)
+    assert info["status"] == 0
+    assert rel(u, x) <= 1e-8
+    assert L.cfem_selftest_copy_timeout(FemContext(meshgen.square_2d(4))._h) == capi.ERR_UNSUPPORTED
