@@ -422,6 +422,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-oracle", action="store_true", help="measure errors against the GPU FP64 solution instead")
     ap.add_argument("--no-multi", action="store_true", help="skip the 64-case multi-RHS leg")
+    ap.add_argument("--no-configs", action="store_true", help="skip the adjoint and dynamics legs")
     ap.add_argument("--workload", default="cantilever", choices=["cantilever", "multi_rhs", "batch", "adjoint", "dynamics"],
                     help="cantilever: the headline solve; the others measure the remaining configurations "
                          "(one JSON line each, single GPU)")
@@ -593,6 +594,9 @@ def main():
     }
     if rank == 0 and world == 1 and not args.no_multi:
         line["multi_rhs"] = multi_rhs_leg(torch, check_oracle=not args.no_oracle)
+    if rank == 0 and world == 1 and not args.no_configs:
+        line["adjoint"] = adjoint_leg(check_oracle=not args.no_oracle)
+        line["dynamics"] = dynamics_leg()
     if rank == 0 and world == 1 and not args.no_cpu:
         # reference rule iteration count on the GPU (FP32, gamma < 1e-8 gamma0) for the extrapolation
         _, ir = ctx.pcg(f_dev, out=u_dev, precision="fp32", tol=1e-8, stop_rule="reference",
@@ -697,6 +701,111 @@ def multi_rhs_leg(torch, check_oracle: bool = True, k: int = 64):
             xo, _ = o.pcg(F[i], tol=1e-12, rule=1)
             errs.append(float(np.linalg.norm(U[i] - xo) / np.linalg.norm(xo)))
         out["rel_err_vs_oracle_cases_0_and_last"] = max(errs)
+    ctx.close()
+    return out
+
+
+def adjoint_leg(check_oracle: bool = True):
+    """Adjoint gradient on the tet cantilever 32x32x128 x 6 (786,432 tets,
+    421,443 DOF) with E_e = 2e7 exp(0.5 z_e), z_e standard normal (seed 3);
+    loss = f.u + 1/2 sum over 500 surface sensors |u_s - u_obs|^2, u_obs from a
+    second modulus field (seed 4). Forward and adjoint solves by FP32 PCG +
+    FP64 refinement to a true relative residual of 1e-13; dL/dE against the
+    FP64 oracle's adjoint gradient of the same mesh and against central
+    differences along a random direction (relative step 1e-4)."""
+    from cudafemproject_gb300 import meshgen
+    from cudafemproject_gb300.solver import FemContext
+    p = meshgen.box_3d(32, 32, 128, traction=(0.0, -1e3, 0.0))
+    rng = np.random.default_rng(3)
+    young = 2e7 * np.exp(0.5 * rng.standard_normal(p.n_elems))
+    surf = np.nonzero((p.nodes[:, 0] <= 1e-9) | (p.nodes[:, 0] >= 1 - 1e-9) | (p.nodes[:, 1] <= 1e-9) |
+                      (p.nodes[:, 1] >= 1 - 1e-9) | (p.nodes[:, 2] >= 4 - 1e-9))[0]
+    sensors = rng.choice(surf, size=500, replace=False)
+    young_obs = 2e7 * np.exp(0.5 * np.random.default_rng(4).standard_normal(p.n_elems))
+    kw = dict(precision="fp32_refine", tol=0.4, stop_rule="residual", outer_tol=1e-13, max_outer=200, max_iter=40000)
+    p.elem_E = young_obs
+    ctx = FemContext(p, semantics="consistent")
+    f = ctx.rhs()
+    u_obs = np.asarray(ctx.pcg(f, **kw)[0]).reshape(-1, 3)[sensors]
+    p.elem_E = young
+    ctx.set_young(young)
+    ctx.pcg(f, **kw)
+    u, inf_f = ctx.pcg(f, **kw)
+    g = f.copy().reshape(-1, 3)
+    g[sensors] += np.asarray(u).reshape(-1, 3)[sensors] - u_obs
+    dE, df, inf_a = ctx.adjoint(u, g.ravel(), **kw)
+
+    def loss(uu):
+        uu = np.asarray(uu).reshape(-1, 3)
+        return float(f @ uu.ravel() + 0.5 * np.sum((uu[sensors] - u_obs) ** 2))
+
+    v = np.random.default_rng(7).standard_normal(p.n_elems) * young
+    h = 1e-4
+    ctx.set_young(young + h * v)
+    lp = loss(ctx.pcg(f, **kw)[0])
+    ctx.set_young(young - h * v)
+    lm = loss(ctx.pcg(f, **kw)[0])
+    ctx.set_young(young)
+    fd = (lp - lm) / (2 * h)
+    out = {"workload": "tet cantilever 32x32x128 x 6 (786,432 tets, 421,443 DOF), E_e = 2e7 exp(0.5 z_e) seed 3, "
+                       "compliance + 500-sensor misfit (u_obs from field seed 4)",
+           "forward_ms": round(inf_f["solve_ms"], 2), "adjoint_ms": round(inf_a["solve_ms"], 2),
+           "fd_directional_rel_err": abs(fd - float(dE @ v)) / abs(float(dE @ v))}
+    ctx.close()
+    if check_oracle:
+        oracle = _oracle()
+        o = oracle.Oracle(p, consistent=True).assemble()
+        uo, _ = o.pcg(f, tol=1e-12, rule=1)
+        go = f.copy().reshape(-1, 3)
+        go[sensors] += uo.reshape(-1, 3)[sensors] - u_obs
+        lam, _ = o.pcg(go.ravel(), tol=1e-12, rule=1)
+        gE = o.grad_E(lam, uo)
+        out["rel_err_vs_oracle_dLdE"] = float(np.linalg.norm(dE - gE) / np.linalg.norm(gE))
+        out["rel_err_vs_oracle_dLdf"] = float(np.linalg.norm(np.asarray(df) - lam) / np.linalg.norm(lam))
+    return out
+
+
+def dynamics_leg():
+    """Elastodynamics on the tet column 1x1x8, 32x32x256 x 6 (1,572,864 tets,
+    839,619 DOF), rho 2000, E 2e7, nu 0.25, base clamped, Ricker point force
+    (25 Hz, -z) at the top centre, consistent semantics. Explicit central
+    difference (lumped mass) at 0.5 x the stability limit (100 power iterations
+    on M_L^-1 K, seed 5): 2000 FP32 and 200 FP64 steps. Implicit Newmark (beta
+    0.25, gamma 0.5), dt 1 ms, warm-started PCG per step: 100 FP32 steps
+    (relative residual 1e-6) and 20 FP64 steps (1e-10)."""
+    from cudafemproject_gb300 import meshgen
+    from cudafemproject_gb300.meshio import WaveletParams
+    from cudafemproject_gb300.solver import FemContext
+    p = meshgen.box_3d(32, 32, 256, lz=8.0, E=2e7, nu=0.25, rho=2000.0, traction=(0.0, 0.0, 0.0),
+                       point_load=("top_centre", (0.0, 0.0, -1.0)))
+    ctx = FemContext(p, semantics="consistent")
+    X = p.nodes[p.elems]
+    vol = np.abs(np.einsum("ij,ij->i", X[:, 1] - X[:, 0], np.cross(X[:, 2] - X[:, 0], X[:, 3] - X[:, 0]))) / 6
+    m = np.zeros(p.n_nodes)
+    np.add.at(m, p.elems.ravel(), np.repeat(p.rho * vol / 4, 4))
+    minv = np.repeat(1.0 / m, 3)
+    x = np.random.default_rng(5).standard_normal(p.n_dof)
+    lam = 0.0
+    for _ in range(100):
+        y = minv * ctx.matvec(x, "fp64")
+        lam = float(np.linalg.norm(y) / np.linalg.norm(x))
+        x = y / np.linalg.norm(y)
+    dt = 0.5 * 2.0 / np.sqrt(lam)
+    w = WaveletParams("ricker", 25.0, 0.0, 1.0)
+    out = {"workload": "tet column 1x1x8, 32x32x256 x 6 (1,572,864 tets, 839,619 DOF), Ricker 25 Hz point force",
+           "explicit_dt": dt}
+    ctx.dyn(0.5, 0.0, dt, 10 * dt * 1.0000001, precision="fp32", wavelet=w)
+    for prec, n in (("fp32", 2000), ("fp64", 200)):
+        _, info = ctx.dyn(0.5, 0.0, dt, n * dt * 1.0000001, precision=prec, wavelet=w)
+        out["explicit_" + prec + "_steps_per_s"] = round(info["steps"] / (info["solve_ms"] * 1e-3), 1)
+    ue32, _ = ctx.dyn(0.5, 0.0, dt, 200 * dt * 1.0000001, precision="fp32", wavelet=w)
+    ue64, _ = ctx.dyn(0.5, 0.0, dt, 200 * dt * 1.0000001, precision="fp64", wavelet=w)
+    out["explicit_fp32_vs_fp64_rel_diff_200_steps"] = float(np.linalg.norm(ue32 - ue64) / np.linalg.norm(ue64))
+    for prec, n, tol in (("fp32", 100, 1e-6), ("fp64", 20, 1e-10)):
+        _, info = ctx.dyn(0.5, 0.5, 1e-3, n * 1e-3 * 1.0000001, precision=prec, wavelet=w, pcg_tol=tol,
+                          stop_rule="residual", warm_start=True)
+        out["implicit_" + prec + "_steps_per_s"] = round(info["steps"] / (info["solve_ms"] * 1e-3), 1)
+        out["implicit_" + prec + "_pcg_iterations_per_step"] = round(info["pcg_iterations"] / info["steps"], 1)
     ctx.close()
     return out
 

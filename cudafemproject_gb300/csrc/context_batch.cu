@@ -325,8 +325,9 @@ extern "C" cfem_status cfem_batch_static_solve(cfem_ctx *ctx, const cfem_solve_p
           if (status[i] == CFEM_OK || status[i] == CFEM_ERR_DIVERGED) continue;
           const bool conv = std::sqrt(rr[i]) <= outer_tol * std::sqrt(ff[i]);
           // the FP64 true residual has a floor near eps64 * ||K|| ||x||: a
-          // refinement step that no longer halves it ends the instance
-          const bool stalled = rr_prev[i] >= 0 && rr[i] > 0.25 * rr_prev[i];
+          // refinement step that no longer reduces it as a step should ends
+          // the instance
+          const bool stalled = rr_prev[i] >= 0 && rr[i] > refine_stall_ratio(p.tol) * rr_prev[i];
           if (conv || stalled || ff[i] == 0.0) { status[i] = CFEM_OK; continue; }
           if (round == max_outer) continue;
           act[i] = 1;

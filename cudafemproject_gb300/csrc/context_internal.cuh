@@ -206,11 +206,9 @@ namespace detail {
 // which its recursive residual drops between FP64 true-residual replacements).
 constexpr double kContinueTol = 0.2;
 // A refinement step whose FP64 residual norm^2 falls by less than this is at
-// the FP64 floor: a restarted step halves the norm at least, a continued one
-// cuts it by about the replacement factor.
-inline double refine_stall_ratio(double tol) {
-  return tol >= kContinueTol ? std::min(0.9, std::max(0.25, 4.0 * tol * tol)) : 0.25;
-}
+// the FP64 floor: a step cuts the norm by about the inner tolerance tol (at
+// least halves it for tol up to 0.25), so the test allows twice that.
+inline double refine_stall_ratio(double tol) { return std::min(0.9, std::max(0.25, 4.0 * tol * tol)); }
 
 struct PcgResult {
   int status = CFEM_OK;

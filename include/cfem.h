@@ -124,7 +124,10 @@ typedef struct cfem_wavelet {
 typedef struct cfem_solve_params {
   int32_t precision;     /* cfem_precision */
   int32_t stop_rule;     /* cfem_stop_rule (inner rule for CFEM_FP32_REFINE) */
-  double tol;            /* reference: 1e-8 static, 1e-4 dynamics */
+  double tol;            /* reference: 1e-8 static, 1e-4 dynamics. CFEM_FP32_REFINE: the inner FP32 PCG's
+                            residual drop per refinement step; from 0.2 up the inner PCG keeps its search
+                            direction across the FP64 true-residual replacements (fastest near 0.3-0.4),
+                            below 0.2 each step restarts it */
   int32_t max_iter;      /* PCG iteration cap (per inner solve) */
   double outer_tol;      /* CFEM_FP32_REFINE: stop when ||f - K x||_2 <= outer_tol ||f||_2 */
   int32_t max_outer;     /* CFEM_FP32_REFINE: refinement step cap */
