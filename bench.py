@@ -422,7 +422,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-oracle", action="store_true", help="measure errors against the GPU FP64 solution instead")
     ap.add_argument("--no-multi", action="store_true", help="skip the 64-case multi-RHS leg")
-    ap.add_argument("--no-configs", action="store_true", help="skip the adjoint and dynamics legs")
+    ap.add_argument("--no-configs", action="store_true", help="skip the adjoint, dynamics and batched-mesh legs")
     ap.add_argument("--workload", default="cantilever", choices=["cantilever", "multi_rhs", "batch", "adjoint", "dynamics"],
                     help="cantilever: the headline solve; the others measure the remaining configurations "
                          "(one JSON line each, single GPU)")
@@ -597,6 +597,7 @@ def main():
     if rank == 0 and world == 1 and not args.no_configs:
         line["adjoint"] = adjoint_leg(check_oracle=not args.no_oracle)
         line["dynamics"] = dynamics_leg()
+        line["batch"] = batch_leg(check_oracle=not args.no_oracle)
     if rank == 0 and world == 1 and not args.no_cpu:
         # reference rule iteration count on the GPU (FP32, gamma < 1e-8 gamma0) for the extrapolation
         _, ir = ctx.pcg(f_dev, out=u_dev, precision="fp32", tol=1e-8, stop_rule="reference",
@@ -808,6 +809,47 @@ def dynamics_leg():
         out["implicit_" + prec + "_pcg_iterations_per_step"] = round(info["pcg_iterations"] / info["steps"], 1)
     ctx.close()
     return out
+
+
+def batch_leg(check_oracle: bool = True):
+    """64 independent tet boxes n x n x 4n, n uniform in 8..40 (seed 2), E
+    log-uniform in [1e6, 1e8], nu uniform in [0.2, 0.4], each clamped at z=0
+    with a traction on its top face: solved together in one persistent launch
+    per kernel (per-instance convergence masks, graph replay) against the same
+    solves one mesh after the other, both FP32 PCG + FP64 refinement (inner
+    1e-4, outer 1e-8). Errors against the FP64 oracle for the two smallest
+    boxes and against GPU FP64 solutions for the two largest."""
+    from cudafemproject_gb300 import meshgen
+    from cudafemproject_gb300.solver import BatchContext, FemContext
+    probs = meshgen.batch_boxes(64, seed=2)
+    kw = dict(precision="fp32_refine", tol=1e-4, stop_rule="residual", outer_tol=1e-8, max_iter=20000)
+    b = BatchContext(probs)
+    b.static_solve(**kw)
+    us, infos = b.static_solve(**kw)
+    ms_b = infos[0]["solve_ms"]
+    b.close()
+    sizes = np.array([p.n_elems for p in probs])
+    small = list(np.argsort(sizes)[:2])
+    large = list(np.argsort(sizes)[-2:])
+    seq, errs = 0.0, {}
+    for i, p in enumerate(probs):
+        ctx = FemContext(p, semantics="consistent")
+        ctx.static_solve(**kw)
+        _, inf = ctx.static_solve(**kw)
+        seq += inf["solve_ms"]
+        if i in large:
+            ref, _ = ctx.static_solve("fp64", tol=1e-13, stop_rule="residual", max_iter=60000, allow_not_converged=True)
+            errs[f"box_{i}_vs_gpu_fp64"] = float(np.linalg.norm(us[i] - ref) / np.linalg.norm(ref))
+        ctx.close()
+    if check_oracle:
+        oracle = _oracle()
+        for i in small:
+            xo, _ = oracle.Oracle(probs[i], consistent=True).assemble().static(tol=1e-12, rule=1)
+            errs[f"box_{i}_vs_oracle"] = float(np.linalg.norm(us[i].ravel() - xo) / np.linalg.norm(xo))
+    return {"workload": f"64 tet boxes n x n x 4n, n uniform in 8..40 (seed 2), E log-uniform [1e6, 1e8], nu uniform "
+                        f"[0.2, 0.4]: {int(sizes.sum())} tets, {sum(p.n_dof for p in probs)} DOF",
+            "batched_ms": round(ms_b, 1), "sequential_ms": round(seq, 1), "speedup_vs_sequential": round(seq / ms_b, 3),
+            "max_iterations": max(i["iterations"] for i in infos), "rel_err": errs}
 
 
 if __name__ == "__main__":
