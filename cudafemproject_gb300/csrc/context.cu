@@ -194,16 +194,24 @@ PcgResult run_pcg_t(cfem_ctx *c, Vecs<T> &V, T cK, T cM, const T *mcoef, int war
     const int64_t launches_before_capture = c->launches;
     CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     try {
+      // directions alternate between pA and pB, A p between u and uB: the
+      // matvec of iteration `it` accumulates into one u buffer and zeroes the
+      // other for iteration it + 1 (the init kernel zeroes u for iteration 0;
+      // chunk is even)
       for (int it = 0; it < c->chunk; ++it) {
         T *pold = (it & 1) ? V.pB.p : V.pA.p;
         T *pnew = (it & 1) ? V.pA.p : V.pB.p;
+        T *ucur = (it & 1) ? V.uB.p : V.u.p;
         MvParams<T> m = mv;
         m.x = V.z.p;
         m.x2 = pold;
         m.xout = pnew;
-        m.y = V.u.p;
+        m.y = ucur;
+        m.yzero = (it & 1) ? V.u.p : V.uB.p;
         launch_mv<T>(c, MV_PCG, m);
-        launch_update<T>(c, vec_params<T>(c, V, pnew, sc));
+        VecParams<T> up = vec_params<T>(c, V, pnew, sc);
+        up.u = ucur;
+        launch_update<T>(c, up);
       }
     } catch (...) {
       cudaGraph_t broken = nullptr;
@@ -685,12 +693,14 @@ void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, co
   c->FB32.alloc(c->nvec);
   c->v64.f.alloc(c->nvec);
   // work vectors
-  for (auto *b : {&c->v64.x, &c->v64.r, &c->v64.z, &c->v64.pA, &c->v64.pB, &c->v64.u, &c->v64.dinv, &c->v64.diagA}) {
+  for (auto *b : {&c->v64.x, &c->v64.r, &c->v64.z, &c->v64.pA, &c->v64.pB, &c->v64.u, &c->v64.uB, &c->v64.dinv,
+                  &c->v64.diagA}) {
     b->alloc(c->nvec);
     b->zero(s);
   }
   c->v64.f.zero(s);
-  for (auto *b : {&c->v32.x, &c->v32.r, &c->v32.z, &c->v32.pA, &c->v32.pB, &c->v32.u, &c->v32.f, &c->v32.dinv, &c->v32.diagA}) {
+  for (auto *b : {&c->v32.x, &c->v32.r, &c->v32.z, &c->v32.pA, &c->v32.pB, &c->v32.u, &c->v32.uB, &c->v32.f,
+                  &c->v32.dinv, &c->v32.diagA}) {
     b->alloc(c->nvec);
     b->zero(s);
   }
@@ -1269,7 +1279,8 @@ cfem_status cfem_profile_matvec(cfem_ctx *ctx, int32_t precision, int32_t n_laun
           mv.x = ctx->v64.z.p;
           mv.x2 = (i & 1) ? ctx->v64.pB.p : ctx->v64.pA.p;
           mv.xout = (i & 1) ? ctx->v64.pA.p : ctx->v64.pB.p;
-          mv.y = ctx->v64.u.p;
+          mv.y = (i & 1) ? ctx->v64.uB.p : ctx->v64.u.p;
+          mv.yzero = (i & 1) ? ctx->v64.u.p : ctx->v64.uB.p;
           launch_mv<double>(ctx, MV_PCG, mv);
         } else {
           MvParams<float> mv = base_mv<float>(ctx);
@@ -1278,7 +1289,8 @@ cfem_status cfem_profile_matvec(cfem_ctx *ctx, int32_t precision, int32_t n_laun
           mv.x = ctx->v32.z.p;
           mv.x2 = (i & 1) ? ctx->v32.pB.p : ctx->v32.pA.p;
           mv.xout = (i & 1) ? ctx->v32.pA.p : ctx->v32.pB.p;
-          mv.y = ctx->v32.u.p;
+          mv.y = (i & 1) ? ctx->v32.uB.p : ctx->v32.u.p;
+          mv.yzero = (i & 1) ? ctx->v32.u.p : ctx->v32.uB.p;
           launch_mv<float>(ctx, MV_PCG, mv);
         }
       }
@@ -1293,14 +1305,21 @@ cfem_status cfem_profile_matvec(cfem_ctx *ctx, int32_t precision, int32_t n_laun
     if (ms_per_launch) *ms_per_launch = ms / n_launches;
     // algorithmic bytes: the operator (stored gradients + 8 bytes of connectivity
     // per element; geometry form: the streamed patch blocks, which hold the
-    // connectivity, scatter tables and coordinates) and four node-vector streams
+    // connectivity, scatter tables and coordinates) and five node-vector
+    // streams (z and p_old read, p and A p written, the next A p zeroed)
     if (bytes_per_launch)
       *bytes_per_launch = (ctx->geo && precision == CFEM_FP32
                                ? (double)ctx->prep.n_patches * ctx->Lg.bytes
                                : (double)ctx->ne * (ctx->ncomp * ts + 8)) +
-                          (double)ctx->nn * ctx->vw * ts * 4;
+                          (double)ctx->nn * ctx->vw * ts * 5;
     // leave the work vectors clean for the next solve
-    if (precision == CFEM_FP64) ctx->v64.u.zero(ctx->stream); else ctx->v32.u.zero(ctx->stream);
+    if (precision == CFEM_FP64) {
+      ctx->v64.u.zero(ctx->stream);
+      ctx->v64.uB.zero(ctx->stream);
+    } else {
+      ctx->v32.u.zero(ctx->stream);
+      ctx->v32.uB.zero(ctx->stream);
+    }
     check_copy_error(ctx);
     return CFEM_OK;
   });

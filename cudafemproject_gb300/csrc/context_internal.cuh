@@ -73,7 +73,7 @@ struct DBuf {
 
 template <typename T>
 struct Vecs {
-  DBuf<T> x, r, z, pA, pB, u, f, dinv, diagA;
+  DBuf<T> x, r, z, pA, pB, u, uB, f, dinv, diagA;  // u, uB: A p of even, odd PCG iterations
 };
 
 struct GraphCache {

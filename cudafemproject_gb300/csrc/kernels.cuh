@@ -97,6 +97,14 @@ __device__ __forceinline__ void stv(T *p, int64_t node, const NodeV<T, VW> &r) {
 }
 
 template <typename T, int VW>
+__device__ __forceinline__ void stv_zero(T *p, int64_t node) {
+  NodeV<T, VW> z;
+#pragma unroll
+  for (int d = 0; d < VW; ++d) z.v[d] = T(0);
+  stv<T, VW>(p, node, z);
+}
+
+template <typename T, int VW>
 __device__ __forceinline__ void atomic_addv(T *p, int64_t node, const NodeV<T, VW> &r, int dim) {
   if constexpr (sizeof(T) == 4 && VW == 4) {
     atomicAdd(reinterpret_cast<float4 *>(p) + node, make_float4(r.v[0], r.v[1], r.v[2], 0.f));
@@ -517,6 +525,7 @@ struct MvParams {
   const T *x3;       // DYN: a
   T *xout;           // PCG: p_new; DYN: d_new (owned nodes only)
   T *y;              // result accumulation (zero on entry)
+  T *yzero;          // PCG: zeroed at the owned nodes (the next iteration's y), or nullptr
   Scalars *sc;       // PCG scalars (single mesh)
   double *partials;  // [gridDim] partial sums of p.Ap
   const double *up_part;  // PCG: r.z, r.r partials of the update before it, n_up blocks
@@ -608,7 +617,10 @@ __global__ void __launch_bounds__(kThreads) k_matvec(MvParams<T> P) {
 #pragma unroll
           for (int d = 0; d < DIM; ++d) v.v[d] += beta * po.v[d];
         }
-        if (i >= own) stv<T, VW>(P.xout, g, v);
+        if (i >= own) {
+          stv<T, VW>(P.xout, g, v);
+          if (P.yzero) stv_zero<T, VW>(P.yzero, g);
+        }
       } else if (MODE == MV_DYN) {
         NodeV<T, VW> vv = ldv<T, VW>(P.x2, g), aa = ldv<T, VW>(P.x3, g);
 #pragma unroll
@@ -779,33 +791,46 @@ __global__ void __launch_bounds__(kThreads) k_pcg_init(VecParams<T> P, int warm)
   }
 }
 
-// alpha = gamma / p.Ap; x += alpha p; r -= alpha u; u = 0; z = M^-1 r; gamma' = r.z
+// alpha = gamma / p.Ap; x += alpha p; r -= alpha u; z = M^-1 r; gamma' = r.z.
+// u is left as it is: the matvec of the next iteration accumulates into the
+// other u buffer, which the matvec before it zeroed (MvParams::yzero).
+// Thread t handles nodes t, t + T, t + 2T, ... (T threads in the grid), U of
+// them per round with all their loads in flight. x, r and M^-1 are not written
+// by the matvec this kernel waits for (its predecessor, the update before it,
+// has completed once that matvec passed its own wait), so the first round's
+// loads of those three go out before the wait.
 template <typename T, int DIM>
 __global__ void __launch_bounds__(kThreads, 2) k_pcg_update(VecParams<T> P) {
   constexpr int VW = DIM == 3 ? 4 : 2;
-  griddep_wait();               // A p and the p.Ap partials come from the matvec before it
-  griddep_launch_dependents();  // the next matvec may start streaming its blocks
-  // U nodes per thread per round, all their loads issued before any is used;
-  // the first round's loads go out before the scalar exchange below, which
-  // they do not depend on
   constexpr int U = sizeof(T) == 4 ? 4 : 2;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x * U;
-  int64_t base = blockIdx.x * (int64_t)blockDim.x * U + threadIdx.x;
+  const int64_t nthr = (int64_t)gridDim.x * blockDim.x;
+  int64_t base = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   NodeV<T, VW> x[U], r[U], p[U], u[U], di[U];
-  auto load_round = [&]() {
+  auto load_own = [&]() {
 #pragma unroll
     for (int q = 0; q < U; ++q) {
-      const int64_t n = base + (int64_t)q * blockDim.x;
+      const int64_t n = base + (int64_t)q * nthr;
       if (n < P.n_nodes) {
         x[q] = ldv<T, VW>(P.x, n);
         r[q] = ldv<T, VW>(P.r, n);
-        p[q] = ldv<T, VW>(P.p, n);
-        u[q] = ldv<T, VW>(P.u, n);
         di[q] = ldv<T, VW>(P.dinv, n);
       }
     }
   };
-  load_round();
+  auto load_mv = [&]() {
+#pragma unroll
+    for (int q = 0; q < U; ++q) {
+      const int64_t n = base + (int64_t)q * nthr;
+      if (n < P.n_nodes) {
+        p[q] = ldv<T, VW>(P.p, n);
+        u[q] = ldv<T, VW>(P.u, n);
+      }
+    }
+  };
+  load_own();
+  griddep_wait();               // A p and the p.Ap partials come from the matvec before it
+  griddep_launch_dependents();  // the next matvec may start streaming its blocks
+  load_mv();
   // thread 0 reads the scalars while every thread loads the matvec's partials
   // (see pcg_matvec_scalars); alpha = gamma / sigma in thread 0, shared
   Scalars *s = P.sc;
@@ -835,15 +860,18 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg_update(VecParams<T> P) {
   const double alpha_d = red_pcg[18];
   const T alpha = (T)alpha_d;
   DotAcc<T> acc[2];
-  for (bool first = true; base < P.n_nodes; base += stride, first = false) {
-    if (!first) load_round();
+  for (bool first = true; base < P.n_nodes; base += U * nthr, first = false) {
+    if (!first) {
+      load_own();
+      load_mv();
+    }
 #pragma unroll
     for (int q = 0; q < U; ++q) {
-      const int64_t n = base + (int64_t)q * blockDim.x;
+      const int64_t n = base + (int64_t)q * nthr;
       if (n >= P.n_nodes) continue;
-      NodeV<T, VW> z, zero;
+      NodeV<T, VW> z;
 #pragma unroll
-      for (int d = 0; d < VW; ++d) { zero.v[d] = 0; z.v[d] = 0; }
+      for (int d = 0; d < VW; ++d) z.v[d] = 0;
       T rz = 0, rr = 0;
 #pragma unroll
       for (int d = 0; d < DIM; ++d) {
@@ -858,7 +886,6 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg_update(VecParams<T> P) {
       stv<T, VW>(P.x, n, x[q]);
       stv<T, VW>(P.r, n, r[q]);
       stv<T, VW>(P.z, n, z);
-      stv<T, VW>(P.u, n, zero);
     }
   }
   // r.z, r.r partials; the next matvec forms gamma, beta and the stopping test

@@ -63,7 +63,10 @@ __global__ void __launch_bounds__(kFanThreads) k_matvec_fan(MvParams<T> P, FanPa
 #pragma unroll
           for (int d = 0; d < DIM; ++d) v.v[d] += beta * po.v[d];
         }
-        if (i >= own) stv<T, VW>(P.xout, g, v);
+        if (i >= own) {
+          stv<T, VW>(P.xout, g, v);
+          if (P.yzero) stv_zero<T, VW>(P.yzero, g);
+        }
       } else if (MODE == MV_DYN) {
         NodeV<T, VW> vv = ldv<T, VW>(P.x2, g), aa = ldv<T, VW>(P.x3, g);
 #pragma unroll
@@ -79,53 +82,80 @@ __global__ void __launch_bounds__(kFanThreads) k_matvec_fan(MvParams<T> P, FanPa
       sb[i] = (uint8_t)b;
     }
     __syncthreads();
-    // 2. fans
+    // 2. fans: differences to P once per fan node, each tet's stiffness forces
+    //    accumulated into the forces on Q, R_j, R_j+1 (tet_forces_acc); the
+    //    force on P is minus the sum of the others (the stiffness forces of a
+    //    tet sum to zero), plus the mass forces when there is a mass term
     for (int fl = threadIdx.x; fl < nf; fl += blockDim.x) {
       const int64_t f = f0 + fl;
       const int len = F.slot[(size_t)(kFanSlots - 1) * F.fstride + f];
-      T uv[NS][DIM], fv[NS][DIM];
+      T u0[DIM], du[NS][DIM], fv[NS][DIM], corr[DIM];
+      {
+        const NodeV<T, VW> s0 = ldv<T, VW>(sp, F.slot[f]);
 #pragma unroll
-      for (int k = 0; k < NS; ++k) {
+        for (int d = 0; d < DIM; ++d) {
+          u0[d] = s0.v[d];
+          corr[d] = 0;
+        }
+      }
+#pragma unroll
+      for (int k = 1; k < NS; ++k) {
         NodeV<T, VW> s;
 #pragma unroll
         for (int d = 0; d < VW; ++d) s.v[d] = 0;
         if (k < len + 3) s = ldv<T, VW>(sp, F.slot[(size_t)k * F.fstride + f]);
 #pragma unroll
         for (int d = 0; d < DIM; ++d) {
-          uv[k][d] = s.v[d];
+          du[k][d] = s.v[d] - u0[d];
           fv[k][d] = 0;
         }
       }
       const int64_t fe0 = P.mcoef ? F.fan_elem_off[f] : 0;
-      T e_fan = 0;
+      const T lamk = P.cK * lam, muk = P.cK * mu;
 #pragma unroll
       for (int j = 0; j < kFanMax; ++j) {
         if (j < len) {
           T G[9];
 #pragma unroll
           for (int k = 0; k < 9; ++k) G[k] = Gf[(size_t)(j * 9 + k) * F.fstride + f];
-          T u[4][DIM], fe[4][DIM];
+          tet_forces_acc<T>(du[1], du[2 + j], du[3 + j], G, lamk, muk, fv[1], fv[2 + j], fv[3 + j]);
+          if (P.mcoef) {  // f_a += m (u_a + sum_b u_b) on all four vertices
+            const T mc = P.cM * P.mcoef[fe0 + j];
 #pragma unroll
-          for (int d = 0; d < DIM; ++d) {
-            u[0][d] = uv[0][d];
-            u[1][d] = uv[1][d];
-            u[2][d] = uv[2 + j][d];
-            u[3][d] = uv[3 + j][d];
-          }
-          const T mc = P.mcoef ? P.cM * P.mcoef[fe0 + j] : T(0);
-          element_force<T, DIM>(u, G, lam, mu, P.cK, mc, fe);
-#pragma unroll
-          for (int d = 0; d < DIM; ++d) {
-            if (MODE == MV_PCG) e_fan += u[0][d] * fe[0][d] + u[1][d] * fe[1][d] + u[2][d] * fe[2][d] + u[3][d] * fe[3][d];
-            fv[0][d] += fe[0][d];
-            fv[1][d] += fe[1][d];
-            fv[2 + j][d] += fe[2][d];
-            fv[3 + j][d] += fe[3][d];
+            for (int d = 0; d < DIM; ++d) {
+              const T a0 = u0[d], a1 = du[1][d] + u0[d], a2 = du[2 + j][d] + u0[d], a3 = du[3 + j][d] + u0[d];
+              const T sum = a0 + a1 + a2 + a3;
+              const T m0 = mc * (a0 + sum), m1 = mc * (a1 + sum), m2 = mc * (a2 + sum), m3 = mc * (a3 + sum);
+              fv[1][d] += m1;
+              fv[2 + j][d] += m2;
+              fv[3 + j][d] += m3;
+              corr[d] += m0 + m1 + m2 + m3;
+            }
           }
         }
       }
+      // P: corr - sum of the others; p.Ap of the fan = u_P.corr + sum_k du_k.f_k
+      T fP[DIM], e_fan = 0;
 #pragma unroll
-      for (int k = 0; k < NS; ++k)
+      for (int d = 0; d < DIM; ++d) {
+        T t = 0;
+#pragma unroll
+        for (int k = 1; k < NS; ++k) t += fv[k][d];
+        fP[d] = corr[d] - t;
+        if (MODE == MV_PCG) {
+          e_fan += u0[d] * corr[d];
+#pragma unroll
+          for (int k = 1; k < NS; ++k) e_fan += du[k][d] * fv[k][d];
+        }
+      }
+      {
+        NodeV<T, VW> o;
+#pragma unroll
+        for (int d = 0; d < VW; ++d) o.v[d] = d < DIM ? fP[d] : T(0);
+        stv<T, VW>(fs, fl, o);
+      }
+#pragma unroll
+      for (int k = 1; k < NS; ++k)
         if (k < len + 3) {
           NodeV<T, VW> o;
 #pragma unroll

@@ -349,7 +349,10 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
 #pragma unroll
           for (int d = 0; d < DIM; ++d) v.v[d] += beta * w.v[d];
         }
-        if (i >= own) stv<T, VW>(P.xout, nodes[i], v);
+        if (i >= own) {
+          stv<T, VW>(P.xout, nodes[i], v);
+          if (P.yzero) stv_zero<T, VW>(P.yzero, nodes[i]);
+        }
         const unsigned bb = bits[i];
         NodeV<T, VW> m;
 #pragma unroll
@@ -400,7 +403,10 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
 #pragma unroll
             for (int d = 0; d < DIM; ++d) v[q].v[d] += beta * w[q].v[d];
           }
-          if (i >= own) stv<T, VW>(P.xout, gi[q], v[q]);
+          if (i >= own) {
+            stv<T, VW>(P.xout, gi[q], v[q]);
+            if (P.yzero) stv_zero<T, VW>(P.yzero, gi[q]);
+          }
         } else if (MODE == MV_DYN) {
 #pragma unroll
           for (int d = 0; d < DIM; ++d) v[q].v[d] += P.c1 * w[q].v[d] + P.c2 * a3[q].v[d];
