@@ -174,79 +174,139 @@ PcgResult run_pcg_t(cfem_ctx *c, Vecs<T> &V, T cK, T cM, const T *mcoef, int war
     launch_mv<T>(c, MV_PLAIN, mv);
   }
   launch_init<T>(c, vec_params<T>(c, V, V.pA.p, sc), warm);
-  if (cont_p) {
+  if (cont_p && cont_gamma_prev > 0) {
     // Continuation of an earlier run on a new residual: its last direction
     // p_last stays, and the first direction becomes the conjugate-gradient
     // step from it, z + (gamma / gamma_prev) p_last, folded into z here (the
     // first matvec takes p = z).
-    CK(cudaMemcpyAsync(c->h_sc, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-    if (!c->h_sc->done && cont_gamma_prev > 0) {
-      const T beta = (T)(c->h_sc->gamma / cont_gamma_prev);
-      k_add_scaled<T><<<nblk(c->nvec), kThreads, 0, c->stream>>>(c->nvec, beta, cont_p, V.z.p);
-      CKL();
-    }
+    k_fold_direction<T><<<nblk(c->nvec), kThreads, 0, c->stream>>>(c->nvec, sc, cont_gamma_prev, cont_p, V.z.p);
+    CKL();
+    c->launches += 1;
   }
   GraphCache &gc = sizeof(T) == 8 ? c->graph64 : c->graph32;
+  // directions alternate between pA and pB, A p between u and uB: the matvec
+  // of iteration `it` accumulates into one u buffer and zeroes the other for
+  // iteration it + 1 (the init kernel zeroes u for iteration 0; chunk is even)
+  auto capture_iterations = [&](unsigned long long cond) {
+    for (int it = 0; it < c->chunk; ++it) {
+      T *pold = (it & 1) ? V.pB.p : V.pA.p;
+      T *pnew = (it & 1) ? V.pA.p : V.pB.p;
+      T *ucur = (it & 1) ? V.uB.p : V.u.p;
+      MvParams<T> m = mv;
+      m.x = V.z.p;
+      m.x2 = pold;
+      m.xout = pnew;
+      m.y = ucur;
+      m.yzero = (it & 1) ? V.u.p : V.uB.p;
+      launch_mv<T>(c, MV_PCG, m);
+      VecParams<T> up = vec_params<T>(c, V, pnew, sc);
+      up.u = ucur;
+      up.cond = cond;
+      up.cond_role = (it == 0 ? 1 : 0) | (it == c->chunk - 1 ? 2 : 0);
+      up.cond_chunk = c->chunk;
+      launch_update<T>(c, up);
+    }
+  };
   if (!gc.exec || gc.key0 != (const void *)mcoef || gc.key1 != (double)cK || gc.key2 != (double)cM) {
     gc.reset();
-    cudaGraph_t graph;
     const int64_t launches_before_capture = c->launches;
-    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    try {
-      // directions alternate between pA and pB, A p between u and uB: the
-      // matvec of iteration `it` accumulates into one u buffer and zeroes the
-      // other for iteration it + 1 (the init kernel zeroes u for iteration 0;
-      // chunk is even)
-      for (int it = 0; it < c->chunk; ++it) {
-        T *pold = (it & 1) ? V.pB.p : V.pA.p;
-        T *pnew = (it & 1) ? V.pA.p : V.pB.p;
-        T *ucur = (it & 1) ? V.uB.p : V.u.p;
-        MvParams<T> m = mv;
-        m.x = V.z.p;
-        m.x2 = pold;
-        m.xout = pnew;
-        m.y = ucur;
-        m.yzero = (it & 1) ? V.u.p : V.uB.p;
-        launch_mv<T>(c, MV_PCG, m);
-        VecParams<T> up = vec_params<T>(c, V, pnew, sc);
-        up.u = ucur;
-        launch_update<T>(c, up);
+    // Preferred: the iterations inside a CUDA-graph WHILE node, so a solve is
+    // one graph launch and the loop runs without host round trips. Where the
+    // runtime does not build it, a graph of `chunk` iterations that the host
+    // relaunches until the device flag says done.
+    if (!c->host_loop) {
+      cudaGraph_t graph = nullptr;
+      cudaGraphExec_t exec = nullptr;
+      cudaGraphConditionalHandle h = 0;
+      bool ok = cudaGraphCreate(&graph, 0) == cudaSuccess &&
+                cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+      cudaGraph_t body = nullptr;
+      if (ok) {
+        cudaGraphNodeParams np{};
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = h;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        cudaGraphNode_t node;
+        ok = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np) == cudaSuccess;
+        if (ok) body = np.conditional.phGraph_out[0];
       }
-    } catch (...) {
-      cudaGraph_t broken = nullptr;
-      cudaStreamEndCapture(c->stream, &broken);
-      if (broken) cudaGraphDestroy(broken);
+      if (ok) ok = cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0,
+                                                 cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+      if (ok) {
+        try {
+          capture_iterations(h);
+        } catch (...) {
+          ok = false;
+        }
+        cudaGraph_t captured = nullptr;
+        if (cudaStreamEndCapture(c->stream, &captured) != cudaSuccess) ok = false;
+      }
+      if (ok) ok = cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess;
+      if (graph) cudaGraphDestroy(graph);
       (void)cudaGetLastError();
-      throw;
+      if (ok) {
+        gc.exec = exec;
+        gc.device_loop = true;
+      } else if (exec) {
+        cudaGraphExecDestroy(exec);
+      }
     }
-    CK(cudaStreamEndCapture(c->stream, &graph));
+    if (!gc.exec) {
+      cudaGraph_t graph;
+      CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+      try {
+        capture_iterations(0);
+      } catch (...) {
+        cudaGraph_t broken = nullptr;
+        cudaStreamEndCapture(c->stream, &broken);
+        if (broken) cudaGraphDestroy(broken);
+        (void)cudaGetLastError();
+        throw;
+      }
+      CK(cudaStreamEndCapture(c->stream, &graph));
+      CK(cudaGraphInstantiate(&gc.exec, graph, 0));
+      cudaGraphDestroy(graph);
+      gc.device_loop = false;
+    }
     c->launches = launches_before_capture;
-    CK(cudaGraphInstantiate(&gc.exec, graph, 0));
-    cudaGraphDestroy(graph);
     gc.key0 = mcoef;
     gc.key1 = cK;
     gc.key2 = cM;
   }
   PcgResult res;
-  // Every replay advances the iteration count by `chunk` unless the device
-  // flag is set; the cap below only guards against a stalled recurrence.
-  const int64_t max_launches = (int64_t)h.maxit / c->chunk + 16;
-  int last_iter = -1, stalled = 0;
-  for (int64_t launch = 0;; ++launch) {
-    if (launch > max_launches || stalled > 4) {
+  if (gc.device_loop) {
+    CK(cudaGraphLaunch(gc.exec, c->stream));
+    CK(cudaMemcpyAsync(c->h_sc, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->launches += (int64_t)2 * c->chunk * c->h_sc->loops;
+    if (c->verbose)
+      std::printf("iteration %d gamma %.6e gamma0 %.6e (%d loops)\n", c->h_sc->iter, c->h_sc->gamma, c->h_sc->gamma0,
+                  c->h_sc->loops);
+    if (!c->h_sc->done) {
       check_copy_error(c);
       throw Fail{CFEM_ERR_CUDA, "PCG recurrence stopped advancing on the device"};
     }
-    CK(cudaGraphLaunch(gc.exec, c->stream));
-    c->launches += 2 * c->chunk;
-    CK(cudaMemcpyAsync(c->h_sc, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-    if (c->verbose)
-      std::printf("iteration %d gamma %.6e gamma0 %.6e\n", c->h_sc->iter, c->h_sc->gamma, c->h_sc->gamma0);
-    if (c->h_sc->done) break;
-    stalled = c->h_sc->iter == last_iter ? stalled + 1 : 0;
-    last_iter = c->h_sc->iter;
+  } else {
+    // Every replay advances the iteration count by `chunk` unless the device
+    // flag is set; the cap below only guards against a stalled recurrence.
+    const int64_t max_launches = (int64_t)h.maxit / c->chunk + 16;
+    int last_iter = -1, stalled = 0;
+    for (int64_t launch = 0;; ++launch) {
+      if (launch > max_launches || stalled > 4) {
+        check_copy_error(c);
+        throw Fail{CFEM_ERR_CUDA, "PCG recurrence stopped advancing on the device"};
+      }
+      CK(cudaGraphLaunch(gc.exec, c->stream));
+      c->launches += 2 * c->chunk;
+      CK(cudaMemcpyAsync(c->h_sc, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, c->stream));
+      CK(cudaStreamSynchronize(c->stream));
+      if (c->verbose)
+        std::printf("iteration %d gamma %.6e gamma0 %.6e\n", c->h_sc->iter, c->h_sc->gamma, c->h_sc->gamma0);
+      if (c->h_sc->done) break;
+      stalled = c->h_sc->iter == last_iter ? stalled + 1 : 0;
+      last_iter = c->h_sc->iter;
+    }
   }
   check_copy_error(c);
   res.iters = c->h_sc->iter;

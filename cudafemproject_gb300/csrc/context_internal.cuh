@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <functional>
 #include <memory>
@@ -78,6 +79,7 @@ struct Vecs {
 
 struct GraphCache {
   cudaGraphExec_t exec = nullptr;
+  bool device_loop = false;  // exec is a WHILE node around the iterations (one launch per solve)
   const void *key0 = nullptr;
   double key1 = 0, key2 = 0;
   ~GraphCache() { reset(); }
@@ -165,7 +167,10 @@ struct cfem_ctx {
   double *h_rr = nullptr;
   int grid_mv = 0, grid_vec = 0;
   size_t smem64 = 0, smem32 = 0;
-  int chunk = 16;
+  int chunk = 16;  // PCG iterations per graph body (even: the A p buffers alternate)
+  // run the PCG iterations from the host, `chunk` per graph launch, instead of
+  // inside a graph WHILE node (CFEM_HOST_LOOP set in the environment)
+  bool host_loop = std::getenv("CFEM_HOST_LOOP") != nullptr;
   MultiState *multi = nullptr;
   // batch of independent meshes (cfem_create_batch); n_inst == 0 for one mesh
   int n_inst = 0;

@@ -40,12 +40,13 @@ struct Scalars {
   int rule, maxit, iter, done;  // done: 0 running, 1 converged, 2 diverged, 3 iteration cap
   unsigned int count_spare, count_up;  // count_up: grid-sum ticket of the init kernel
   int u_iter;  // iterations completed when the last update ran (-1: none since the init kernel)
-  int pad1;
+  int loops;   // device-side loop: bodies started in this run (pcg_matvec_scalars)
   // alpha = gamma / sigma (set by CTA 0 of the update from the matvec's block
   // partials), beta = gamma / gamma_prev (set by CTA 0 of the matvec from the
   // update's block partials, 0 before the first direction): every CTA derives
   // them identically, so no thread divides differently
   double alpha, beta;
+  int loop_ok, pad2;  // device-side loop: loops within the cap
 };
 
 struct DynState {
@@ -375,6 +376,7 @@ __device__ __forceinline__ double partials_total(const double *red, int k) {
 // loads, and shares the result through red (24 doubles of shared scratch):
 // the CTAs of a grid reading the same line thread by thread would queue at
 // one L2 slice.
+
 template <typename T>
 __device__ __forceinline__ bool pcg_matvec_scalars(Scalars *s, const double *up_part, int n_up, T &beta,
                                                    double *red) {
@@ -742,6 +744,11 @@ struct VecParams {
   const double *mv_part;  // update: p.Ap partials of the matvec before it, n_mv blocks
   int n_mv;
   double *up_part;        // update: its own r.z, r.r partials [grid][2]
+  // PCG iterations inside a CUDA-graph WHILE node (0: loop on the host); see
+  // k_pcg_update
+  unsigned long long cond;
+  int cond_role;   // bit 0: first update of the body, bit 1: last
+  int cond_chunk;  // iterations per body
 };
 
 // r = f - u (warm) or f; x = 0 unless warm; z = M^-1 r; u = 0; gamma0 = r.z
@@ -830,6 +837,18 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg_update(VecParams<T> P) {
   load_own();
   griddep_wait();               // A p and the p.Ap partials come from the matvec before it
   griddep_launch_dependents();  // the next matvec may start streaming its blocks
+  // Device-side loop (one thread of CTA 0; the updates of a body run one
+  // after another, so no two calls race): the first update of a body counts
+  // the body and clears the condition, the last one sets it to "the matvec
+  // before it found the run not done, and the body count is within
+  // maxit / chunk + 16". A body ends the loop unless its last update sets it,
+  // and the cap ends it whatever the scalars do.
+  const bool cond_thread = P.cond && blockIdx.x == 0 && threadIdx.x == 0;
+  if (cond_thread && (P.cond_role & 1)) {
+    const int nl = ++P.sc->loops;
+    P.sc->loop_ok = nl <= P.sc->maxit / P.cond_chunk + 16;
+    cudaGraphSetConditional(P.cond, 0u);
+  }
   load_mv();
   // thread 0 reads the scalars while every thread loads the matvec's partials
   // (see pcg_matvec_scalars); alpha = gamma / sigma in thread 0, shared
@@ -841,6 +860,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg_update(VecParams<T> P) {
     done0 = s->done;
     gamma = s->gamma;
     it0 = s->iter;
+    if (cond_thread && (P.cond_role & 2)) cudaGraphSetConditional(P.cond, (done0 == 0 && s->loop_ok) ? 1u : 0u);
   }
   partials_warp_sums<1>(P.mv_part, P.n_mv, red_pcg);
   __syncthreads();

@@ -186,11 +186,14 @@ static __global__ void __launch_bounds__(kThreads) k_residual(ResParams P) {
   if (grid_sum_last<2>(acc, P.partials, P.count)) { P.out[0] = acc[0]; P.out[1] = acc[1]; }
 }
 
-// y += a x
+// Continued PCG run: z += (gamma / gamma_prev) p_last, gamma from the init
+// kernel's scalars (nothing to do once they say done).
 template <typename T>
-__global__ void k_add_scaled(int64_t n, T a, const T *x, T *y) {
+__global__ void k_fold_direction(int64_t n, const Scalars *sc, double gamma_prev, const T *p_last, T *z) {
+  if (sc->done) return;
+  const T beta = (T)(sc->gamma / gamma_prev);
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i < n) y[i] += a * x[i];
+  if (i < n) z[i] += beta * p_last[i];
 }
 
 // x64 += (double) x32
