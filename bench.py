@@ -579,6 +579,12 @@ def main():
         "accuracy": accuracy,
         "fp64_ms": round(ms64, 3), "speedup_vs_fp64": round(ms64 / ms, 3),
         "pcg_iterations": its, "outer_iterations": infos[-1]["outer_iterations"],
+        # FP32 halo sums use atomics, so the inner iteration count varies a little from run to run
+        "steps_ms": {"min": round(min(times), 3), "median": round(float(np.median(times)), 3),
+                     "max": round(max(times), 3)},
+        "steps_pcg_iterations": {"min": min(i["iterations"] for i in infos),
+                                 "max": max(i["iterations"] for i in infos)},
+        "ps_per_tet_iteration": round(ms * 1e9 / (ctx.counts()["n_elems"] * float(np.mean([i["iterations"] for i in infos]))), 2),
         "fp64_iterations": i64["iterations"],
         "dof_iterations_per_s": round(nd * its / (ms * 1e-3), 1),
         "setup_ms": round(setup_ms, 1),
@@ -829,14 +835,16 @@ def batch_leg(check_oracle: bool = True):
     ms_b = infos[0]["solve_ms"]
     b.close()
     sizes = np.array([p.n_elems for p in probs])
+    tet_its = float(np.dot(sizes, [i["iterations"] for i in infos]))
     small = list(np.argsort(sizes)[:2])
     large = list(np.argsort(sizes)[-2:])
-    seq, errs = 0.0, {}
+    seq, errs, seq_its = 0.0, {}, []
     for i, p in enumerate(probs):
         ctx = FemContext(p, semantics="consistent")
         ctx.static_solve(**kw)
         _, inf = ctx.static_solve(**kw)
         seq += inf["solve_ms"]
+        seq_its.append(inf["iterations"])
         if i in large:
             ref, _ = ctx.static_solve("fp64", tol=1e-13, stop_rule="residual", max_iter=60000, allow_not_converged=True)
             errs[f"box_{i}_vs_gpu_fp64"] = float(np.linalg.norm(us[i] - ref) / np.linalg.norm(ref))
@@ -849,7 +857,12 @@ def batch_leg(check_oracle: bool = True):
     return {"workload": f"64 tet boxes n x n x 4n, n uniform in 8..40 (seed 2), E log-uniform [1e6, 1e8], nu uniform "
                         f"[0.2, 0.4]: {int(sizes.sum())} tets, {sum(p.n_dof for p in probs)} DOF",
             "batched_ms": round(ms_b, 1), "sequential_ms": round(seq, 1), "speedup_vs_sequential": round(seq / ms_b, 3),
-            "max_iterations": max(i["iterations"] for i in infos), "rel_err": errs}
+            "max_iterations": max(i["iterations"] for i in infos),
+            # time per tet and inner PCG iteration (the work each instance needs): the batched solve
+            # against the same solves one by one, comparable with the headline solve's
+            "ps_per_tet_iteration": {"batched": round(ms_b * 1e9 / tet_its, 2),
+                                     "sequential": round(seq * 1e9 / float(np.dot(sizes, seq_its)), 2)},
+            "rel_err": errs}
 
 
 if __name__ == "__main__":

@@ -144,7 +144,9 @@ void launch_init(cfem_ctx *c, const VecParams<T> &P, int warm) {
 
 template <typename T>
 void launch_update(cfem_ctx *c, const VecParams<T> &P) {
-  if (c->dim == 3) launch_pdl(k_pcg_update<T, 3>, dim3(c->grid_upd), dim3(kThreads), 0, c->stream, P);
+  if (c->dim == 3 && P.cond) launch_pdl(k_pcg_update<T, 3, true>, dim3(c->grid_upd), dim3(kThreads), 0, c->stream, P);
+  else if (c->dim == 3) launch_pdl(k_pcg_update<T, 3>, dim3(c->grid_upd), dim3(kThreads), 0, c->stream, P);
+  else if (P.cond) k_pcg_update<T, 2, true><<<c->grid_vec, kThreads, 0, c->stream>>>(P);
   else k_pcg_update<T, 2><<<c->grid_vec, kThreads, 0, c->stream>>>(P);
   CKL();
   c->launches += 1;
@@ -354,15 +356,18 @@ void to_internal_f(cfem_ctx *c, const double *src, float *dst, double scale) { t
 void to_caller_d(cfem_ctx *c, const double *src, double *dst) { to_caller_t<double>(c, src, dst); }
 void to_caller_f(cfem_ctx *c, const float *src, double *dst) { to_caller_t<float>(c, src, dst); }
 
-// FP64 true residual r = f - K' x (f, x internal FP64), ||r||^2 and ||f||^2
-// into the device doubles out2[0], out2[1]; queued on the context's stream.
+// FP64 true residual r = f - K' x (f, x internal FP64; x == nullptr stands
+// for x = 0), ||r||^2 and ||f||^2 into the device doubles out2[0], out2[1];
+// queued on the context's stream.
 void true_residual_async(cfem_ctx *c, const double *f, const double *x, double *r, float *r32, double *out2) {
-  MvParams<double> mv = base_mv<double>(c);
-  mv.diagA = c->diagK.p;
-  mv.x = x;
-  mv.y = c->tmp64.p;
   c->tmp64.zero(c->stream);
-  launch_mv<double>(c, MV_PLAIN, mv);
+  if (x) {  // (x == nullptr: x = 0, K' x = 0)
+    MvParams<double> mv = base_mv<double>(c);
+    mv.diagA = c->diagK.p;
+    mv.x = x;
+    mv.y = c->tmp64.p;
+    launch_mv<double>(c, MV_PLAIN, mv);
+  }
   ResParams P{};
   P.nvec = c->nvec;
   P.f = f;
@@ -423,7 +428,7 @@ cfem_status solve_internal(cfem_ctx *c, const cfem_solve_params *prm, cfem_solve
     // x64 = 0; r64 = f; repeat: solve K d = r (FP32), x64 += d, r64 = f - K64 x64
     c->v64.x.zero(c->stream);
     double rr = 0, ff = 0;
-    true_residual(c, c->v64.f.p, c->v64.x.p, c->v64.r.p, c->v32.f.p, rr, ff);
+    true_residual(c, c->v64.f.p, nullptr, c->v64.r.p, c->v32.f.p, rr, ff);  // x = 0: r = f
     const double outer_tol = prm->outer_tol > 0 ? prm->outer_tol : 1e-12;
     const int max_outer = prm->max_outer > 0 ? prm->max_outer : 50;
     int outer = 0, total = 0;

@@ -77,6 +77,12 @@ struct Vecs {
   DBuf<T> x, r, z, pA, pB, u, uB, f, dinv, diagA;  // u, uB: A p of even, odd PCG iterations
 };
 
+inline int pcg_chunk_from_env() {
+  const char *e = std::getenv("CFEM_PCG_CHUNK");
+  const int v = e ? std::atoi(e) : 16;
+  return v < 2 ? 16 : (v + 1) & ~1;
+}
+
 struct GraphCache {
   cudaGraphExec_t exec = nullptr;
   bool device_loop = false;  // exec is a WHILE node around the iterations (one launch per solve)
@@ -167,7 +173,9 @@ struct cfem_ctx {
   double *h_rr = nullptr;
   int grid_mv = 0, grid_vec = 0;
   size_t smem64 = 0, smem32 = 0;
-  int chunk = 16;  // PCG iterations per graph body (even: the A p buffers alternate)
+  // PCG iterations per graph body (even: the A p buffers alternate);
+  // CFEM_PCG_CHUNK overrides it (rounded up to even)
+  int chunk = pcg_chunk_from_env();
   // run the PCG iterations from the host, `chunk` per graph launch, instead of
   // inside a graph WHILE node (CFEM_HOST_LOOP set in the environment)
   bool host_loop = std::getenv("CFEM_HOST_LOOP") != nullptr;

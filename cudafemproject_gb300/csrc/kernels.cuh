@@ -806,7 +806,10 @@ __global__ void __launch_bounds__(kThreads) k_pcg_init(VecParams<T> P, int warm)
 // by the matvec this kernel waits for (its predecessor, the update before it,
 // has completed once that matvec passed its own wait), so the first round's
 // loads of those three go out before the wait.
-template <typename T, int DIM>
+// LOOP: the instance for the graph WHILE node (the condition calls below);
+// the host-loop instance leaves them out, which also keeps it profilable
+// (ncu does not profile kernels that set a graph condition).
+template <typename T, int DIM, bool LOOP = false>
 __global__ void __launch_bounds__(kThreads, 2) k_pcg_update(VecParams<T> P) {
   constexpr int VW = DIM == 3 ? 4 : 2;
   constexpr int U = sizeof(T) == 4 ? 4 : 2;
@@ -843,11 +846,13 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg_update(VecParams<T> P) {
   // before it found the run not done, and the body count is within
   // maxit / chunk + 16". A body ends the loop unless its last update sets it,
   // and the cap ends it whatever the scalars do.
-  const bool cond_thread = P.cond && blockIdx.x == 0 && threadIdx.x == 0;
-  if (cond_thread && (P.cond_role & 1)) {
-    const int nl = ++P.sc->loops;
-    P.sc->loop_ok = nl <= P.sc->maxit / P.cond_chunk + 16;
-    cudaGraphSetConditional(P.cond, 0u);
+  const bool cond_thread = LOOP && blockIdx.x == 0 && threadIdx.x == 0;
+  if constexpr (LOOP) {
+    if (cond_thread && (P.cond_role & 1)) {
+      const int nl = ++P.sc->loops;
+      P.sc->loop_ok = nl <= P.sc->maxit / P.cond_chunk + 16;
+      cudaGraphSetConditional(P.cond, 0u);
+    }
   }
   load_mv();
   // thread 0 reads the scalars while every thread loads the matvec's partials
@@ -860,7 +865,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg_update(VecParams<T> P) {
     done0 = s->done;
     gamma = s->gamma;
     it0 = s->iter;
-    if (cond_thread && (P.cond_role & 2)) cudaGraphSetConditional(P.cond, (done0 == 0 && s->loop_ok) ? 1u : 0u);
+    if constexpr (LOOP)
+      if (cond_thread && (P.cond_role & 2)) cudaGraphSetConditional(P.cond, (done0 == 0 && s->loop_ok) ? 1u : 0u);
   }
   partials_warp_sums<1>(P.mv_part, P.n_mv, red_pcg);
   __syncthreads();

@@ -297,16 +297,23 @@ def test_autotune_patch_elems():
 
 
 
+@pytest.mark.parametrize("loop", ["device", "host"])
 @pytest.mark.parametrize("precision", ["fp32", "fp64"])
-def test_pcg_termination_3d(precision):
+def test_pcg_termination_3d(precision, loop, monkeypatch):
     """Stopping paths of the 3D PCG (bulk-copy FP32 fan matvec, FP64 fan
     matvec) whose scalars pass between the matvec and the update as block
     partials: a zero right-hand side stops before the first update; an
-    iteration cap below, at and across the 16-iteration graph chunk stops at
+    iteration cap below, at and across the 16-iteration graph body stops at
     exactly that count, on the same iterate as the oracle's PCG after as many
-    steps (so every alpha and beta of the recurrence agrees)."""
+    steps (so every alpha and beta of the recurrence agrees). Both loops: the
+    graph WHILE node (default) and the host relaunching 16-iteration graphs
+    (CFEM_HOST_LOOP, read when the context is created)."""
     from cudafemproject_gb300 import capi
     from cudafemproject_gb300.solver import FemContext
+    if loop == "host":
+        monkeypatch.setenv("CFEM_HOST_LOOP", "1")
+    else:
+        monkeypatch.delenv("CFEM_HOST_LOOP", raising=False)
     p = meshgen.box_3d(4, 4, 12, jitter=0.2, seed=4)
     o = O.Oracle(p, consistent=True)
     ctx = FemContext(p, semantics="consistent")
