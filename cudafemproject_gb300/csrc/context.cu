@@ -181,7 +181,8 @@ PcgResult run_pcg_t(cfem_ctx *c, Vecs<T> &V, T cK, T cM, const T *mcoef, int war
     // p_last stays, and the first direction becomes the conjugate-gradient
     // step from it, z + (gamma / gamma_prev) p_last, folded into z here (the
     // first matvec takes p = z).
-    k_fold_direction<T><<<nblk(c->nvec), kThreads, 0, c->stream>>>(c->nvec, sc, cont_gamma_prev, cont_p, V.z.p);
+    if (c->dim == 3) k_fold_direction<T, 3><<<nblk(c->nn), kThreads, 0, c->stream>>>(c->nn, sc, cont_gamma_prev, cont_p, V.z.p);
+    else k_fold_direction<T, 2><<<nblk(c->nn), kThreads, 0, c->stream>>>(c->nn, sc, cont_gamma_prev, cont_p, V.z.p);
     CKL();
     c->launches += 1;
   }
@@ -464,7 +465,7 @@ cfem_status solve_internal(cfem_ctx *c, const cfem_solve_params *prm, cfem_solve
       if (outer == 0) inf.gamma0 = r.gamma0;
       inf.gamma = r.gamma;
       if (r.status == CFEM_ERR_DIVERGED) { status = CFEM_ERR_DIVERGED; break; }
-      k_accumulate<<<nblk(c->nvec), kThreads, 0, c->stream>>>(c->nvec, c->v32.x.p, c->v64.x.p);
+      k_accumulate<<<nblk(c->nvec), kThreads, 0, c->stream>>>(c->nvec, c->v32.x.p, c->v64.x.p, c->vw);
       CKL();
       ++outer;
       true_residual(c, c->v64.f.p, c->v64.x.p, c->v64.r.p, c->v32.f.p, rr, ff);

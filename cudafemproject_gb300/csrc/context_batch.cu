@@ -348,7 +348,7 @@ extern "C" cfem_status cfem_batch_static_solve(cfem_ctx *ctx, const cfem_solve_p
           if (res[i].done == 2) status[i] = CFEM_ERR_DIVERGED;
           rr_prev[i] = rr[i];
         }
-        k_accumulate<<<nblk(c->nvec), kThreads, 0, c->stream>>>(c->nvec, c->v32.x.p, c->v64.x.p);
+        k_accumulate<<<nblk(c->nvec), kThreads, 0, c->stream>>>(c->nvec, c->v32.x.p, c->v64.x.p, c->vw);
         CKL();
         batch_kx(c, B);
         batch_residual(c, B, none, rr, ff);

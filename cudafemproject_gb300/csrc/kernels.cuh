@@ -751,7 +751,11 @@ struct VecParams {
   int cond_chunk;  // iterations per body
 };
 
-// r = f - u (warm) or f; x = 0 unless warm; z = M^-1 r; u = 0; gamma0 = r.z
+// r = f - u (warm) or f; x = 0 unless warm; z = M^-1 r; u = 0; gamma0 = r.z.
+// In 3D the spare fourth lanes carry M^-1 for the update kernel: x.w = M^-1
+// of the x DOF, r.w of the y DOF, z.w (and so p.w, which the matvec copies
+// from z) of the z DOF. Every kernel that reads these vectors for their
+// values uses only the first three lanes.
 template <typename T, int DIM>
 __global__ void __launch_bounds__(kThreads) k_pcg_init(VecParams<T> P, int warm) {
   constexpr int VW = DIM == 3 ? 4 : 2;
@@ -761,6 +765,10 @@ __global__ void __launch_bounds__(kThreads) k_pcg_init(VecParams<T> P, int warm)
     NodeV<T, VW> u = ldv<T, VW>(P.u, n);
 #pragma unroll
     for (int d = 0; d < VW; ++d) { zero.v[d] = 0; r.v[d] = 0; z.v[d] = 0; }
+    if constexpr (DIM == 3) {
+      r.v[3] = di.v[1];
+      z.v[3] = di.v[2];
+    }
     T rz = 0, rr = 0, ff = 0;
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
@@ -776,7 +784,14 @@ __global__ void __launch_bounds__(kThreads) k_pcg_init(VecParams<T> P, int warm)
     stv<T, VW>(P.r, n, r);
     stv<T, VW>(P.z, n, z);
     stv<T, VW>(P.u, n, zero);
-    if (!warm) stv<T, VW>(P.x, n, zero);
+    if constexpr (DIM == 3) {
+      NodeV<T, VW> x = zero;
+      if (warm) x = ldv<T, VW>(P.x, n);
+      x.v[3] = di.v[0];
+      stv<T, VW>(P.x, n, x);
+    } else if (!warm) {
+      stv<T, VW>(P.x, n, zero);
+    }
   }
   double tot[3];
   if (grid_sum_acc<3, T>(acc, tot, P.partials, &P.sc->count_up)) {
@@ -802,10 +817,12 @@ __global__ void __launch_bounds__(kThreads) k_pcg_init(VecParams<T> P, int warm)
 // u is left as it is: the matvec of the next iteration accumulates into the
 // other u buffer, which the matvec before it zeroed (MvParams::yzero).
 // Thread t handles nodes t, t + T, t + 2T, ... (T threads in the grid), U of
-// them per round with all their loads in flight. x, r and M^-1 are not written
-// by the matvec this kernel waits for (its predecessor, the update before it,
-// has completed once that matvec passed its own wait), so the first round's
-// loads of those three go out before the wait.
+// them per round with all their loads in flight. In 3D, M^-1 comes from the
+// fourth lanes of x, r and p (k_pcg_init), so a node costs four loads; in 2D
+// from dinv. x and r (and dinv) are not written by the matvec this kernel
+// waits for (its predecessor, the update before it, has completed once that
+// matvec passed its own wait), so the first round's loads of them go out
+// before the wait.
 // LOOP: the instance for the graph WHILE node (the condition calls below);
 // the host-loop instance leaves them out, which also keeps it profilable
 // (ncu does not profile kernels that set a graph condition).
@@ -823,7 +840,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg_update(VecParams<T> P) {
       if (n < P.n_nodes) {
         x[q] = ldv<T, VW>(P.x, n);
         r[q] = ldv<T, VW>(P.r, n);
-        di[q] = ldv<T, VW>(P.dinv, n);
+        if constexpr (DIM != 3) di[q] = ldv<T, VW>(P.dinv, n);
       }
     }
   };
@@ -898,12 +915,22 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg_update(VecParams<T> P) {
       NodeV<T, VW> z;
 #pragma unroll
       for (int d = 0; d < VW; ++d) z.v[d] = 0;
+      T m[DIM];
+      if constexpr (DIM == 3) {
+        m[0] = x[q].v[3];
+        m[1] = r[q].v[3];
+        m[2] = p[q].v[3];
+        z.v[3] = p[q].v[3];
+      } else {
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) m[d] = di[q].v[d];
+      }
       T rz = 0, rr = 0;
 #pragma unroll
       for (int d = 0; d < DIM; ++d) {
         x[q].v[d] += alpha * p[q].v[d];
         r[q].v[d] -= alpha * u[q].v[d];
-        z.v[d] = r[q].v[d] * di[q].v[d];
+        z.v[d] = r[q].v[d] * m[d];
         rz += r[q].v[d] * z.v[d];
         rr += r[q].v[d] * r[q].v[d];
       }

@@ -186,20 +186,28 @@ static __global__ void __launch_bounds__(kThreads) k_residual(ResParams P) {
   if (grid_sum_last<2>(acc, P.partials, P.count)) { P.out[0] = acc[0]; P.out[1] = acc[1]; }
 }
 
-// Continued PCG run: z += (gamma / gamma_prev) p_last, gamma from the init
-// kernel's scalars (nothing to do once they say done).
-template <typename T>
-__global__ void k_fold_direction(int64_t n, const Scalars *sc, double gamma_prev, const T *p_last, T *z) {
+// Continued PCG run: z += (gamma / gamma_prev) p_last on the DOF lanes (the
+// fourth lane carries M^-1, see k_pcg_init), gamma from the init kernel's
+// scalars (nothing to do once they say done).
+template <typename T, int DIM>
+__global__ void k_fold_direction(int64_t nn, const Scalars *sc, double gamma_prev, const T *p_last, T *z) {
+  constexpr int VW = DIM == 3 ? 4 : 2;
   if (sc->done) return;
   const T beta = (T)(sc->gamma / gamma_prev);
-  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i < n) z[i] += beta * p_last[i];
+  int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (n >= nn) return;
+  NodeV<T, VW> zv = ldv<T, VW>(z, n);
+  const NodeV<T, VW> pv = ldv<T, VW>(p_last, n);
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) zv.v[d] += beta * pv.v[d];
+  stv<T, VW>(z, n, zv);
 }
 
-// x64 += (double) x32
-static __global__ void k_accumulate(int64_t n, const float *x32, double *x64) {
+// x64 += (double) x32 on the DOF lanes (vw 4: the fourth lane of x32 carries
+// M^-1, see k_pcg_init)
+static __global__ void k_accumulate(int64_t n, const float *x32, double *x64, int vw) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i < n) x64[i] += (double)x32[i];
+  if (i < n && !(vw == 4 && (i & 3) == 3)) x64[i] += (double)x32[i];
 }
 
 // ------------------------------------------------------------------ dynamics (GN22)
