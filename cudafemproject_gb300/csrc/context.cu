@@ -65,7 +65,11 @@ void launch_mv_t(cfem_ctx *c, int mode, const MvParams<T> &P) {
         F.L = c->Lg;
         F.evict_first = (double)c->Lg.bytes * c->prep.n_patches > l2_half;
         dim3 g(c->grid_geo), b(kHfanThreads);
-        if (mode == MV_PLAIN) k_matvec_fan_tma<float, MV_PLAIN, true><<<g, b, c->smem_geo, c->stream>>>(P, F);
+        if (P.mcoef && mode == MV_PLAIN)
+          k_matvec_fan_tma<float, MV_PLAIN, true, true><<<g, b, c->smem_geo, c->stream>>>(P, F);
+        else if (P.mcoef && mode == MV_PCG)
+          launch_pdl(k_matvec_fan_tma<float, MV_PCG, true, true>, g, b, c->smem_geo, c->stream, P, F);
+        else if (mode == MV_PLAIN) k_matvec_fan_tma<float, MV_PLAIN, true><<<g, b, c->smem_geo, c->stream>>>(P, F);
         else if (mode == MV_PCG) launch_pdl(k_matvec_fan_tma<float, MV_PCG, true>, g, b, c->smem_geo, c->stream, P, F);
         else launch_pdl(k_matvec_fan_tma<float, MV_DYN, true>, g, b, c->smem_geo, c->stream, P, F);
         CKL();
@@ -73,7 +77,11 @@ void launch_mv_t(cfem_ctx *c, int mode, const MvParams<T> &P) {
         return;
       }
       dim3 g(c->grid_ft32), b(kHfanThreads);
-      if (mode == MV_PLAIN) k_matvec_fan_tma<float, MV_PLAIN><<<g, b, c->smem_ft32, c->stream>>>(P, F);
+      if (P.mcoef && mode == MV_PLAIN)
+        k_matvec_fan_tma<float, MV_PLAIN, false, true><<<g, b, c->smem_ft32, c->stream>>>(P, F);
+      else if (P.mcoef && mode == MV_PCG)
+        launch_pdl(k_matvec_fan_tma<float, MV_PCG, false, true>, g, b, c->smem_ft32, c->stream, P, F);
+      else if (mode == MV_PLAIN) k_matvec_fan_tma<float, MV_PLAIN><<<g, b, c->smem_ft32, c->stream>>>(P, F);
       else if (mode == MV_PCG) launch_pdl(k_matvec_fan_tma<float, MV_PCG>, g, b, c->smem_ft32, c->stream, P, F);
       else launch_pdl(k_matvec_fan_tma<float, MV_DYN>, g, b, c->smem_ft32, c->stream, P, F);
       CKL();
@@ -829,7 +837,9 @@ void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, co
     if (c->smem_ft32 + 8192 > (size_t)smem_optin) c->fan_tma = false;
     if (c->fan_tma) {
       for (const void *k : {(const void *)k_matvec_fan_tma<float, MV_PLAIN>, (const void *)k_matvec_fan_tma<float, MV_PCG>,
-                            (const void *)k_matvec_fan_tma<float, MV_DYN>})
+                            (const void *)k_matvec_fan_tma<float, MV_DYN>,
+                            (const void *)k_matvec_fan_tma<float, MV_PLAIN, false, true>,
+                            (const void *)k_matvec_fan_tma<float, MV_PCG, false, true>})
         CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin - 8192));
       int o32 = 1;
       CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o32, k_matvec_fan_tma<float, MV_PCG>, kHfanThreads, c->smem_ft32));
@@ -841,7 +851,9 @@ void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, co
       const size_t smem_max = fan_tma_smem_bytes(fan_geo_block_layout(P.np_max, true), sizeof(float));
       for (const void *k : {(const void *)k_matvec_fan_tma<float, MV_PLAIN, true>,
                             (const void *)k_matvec_fan_tma<float, MV_PCG, true>,
-                            (const void *)k_matvec_fan_tma<float, MV_DYN, true>})
+                            (const void *)k_matvec_fan_tma<float, MV_DYN, true>,
+                            (const void *)k_matvec_fan_tma<float, MV_PLAIN, true, true>,
+                            (const void *)k_matvec_fan_tma<float, MV_PCG, true, true>})
         CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max));
     }
   }

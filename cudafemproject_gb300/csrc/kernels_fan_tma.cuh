@@ -196,7 +196,10 @@ struct FanTmaParams {
   long long wait_limit;
 };
 
-template <typename T, int MODE, bool GEO = false>
+// MASS: the instance for operators with a consistent mass term (P.mcoef set;
+// implicit dynamics), kept apart so that the static instance carries none of
+// its registers.
+template <typename T, int MODE, bool GEO = false, bool MASS = false>
 // (3 CTAs per SM: the shared memory of a CTA allows 3, the register bound makes them fit)
 __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> P, FanTmaParams F) {
   static_assert(sizeof(T) == 4, "patch blocks are FP32");
@@ -467,7 +470,7 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
           load_tet_G(B + L.g_off, threadIdx.x, jj, G);
         }
       };
-      if (P.mcoef == nullptr) {
+      if constexpr (!MASS) {
         const T lamk = lam * P.cK, muk = mu * P.cK;
 #pragma unroll
         for (int k = 1; k < 6; ++k)
