@@ -446,13 +446,16 @@ cfem_status solve_internal(cfem_ctx *c, const cfem_solve_params *prm, cfem_solve
     int cont_iters = 0;  // iterations of the previous FP32 run (0: start the next one afresh)
     double cont_gprev = 0;
     const double stall = refine_stall_ratio(prm->tol);
+    int stalls = 0;
     while (outer < max_outer) {
       if (std::sqrt(rr) <= outer_tol * std::sqrt(ff)) { status = CFEM_OK; break; }
-      // The FP64 true residual has a floor near eps64 * ||K|| ||x||; once a
-      // refinement step no longer reduces it as a step should (halves it; a
-      // continued step reduces it by about the replacement factor tol) the
-      // iterate is converged in FP64.
-      if (rr_prev >= 0 && rr > stall * rr_prev) { status = CFEM_OK; break; }
+      // The FP64 true residual has a floor near eps64 * ||K|| ||x||; once two
+      // refinement steps in a row no longer reduce it as a step should (halve
+      // it; a continued step reduces it by about the replacement factor tol)
+      // the iterate is converged in FP64. (One such step alone can be an FP32
+      // run that ended early, well above the floor.)
+      stalls = rr_prev >= 0 && rr > stall * rr_prev ? stalls + 1 : 0;
+      if (stalls >= 2) { status = CFEM_OK; break; }
       rr_prev = rr;
       // With a loose inner tolerance (a residual-replacement factor, at least
       // kContinueTol), from the second step on the FP32 PCG continues with its

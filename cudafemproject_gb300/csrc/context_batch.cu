@@ -299,6 +299,7 @@ extern "C" cfem_status cfem_batch_static_solve(cfem_ctx *ctx, const cfem_solve_p
     CK(cudaEventRecord(c->ev0, c->stream));
     std::vector<int> iters(n, 0), outer(n, 0), status(n, CFEM_ERR_NOT_CONVERGED), act(n, 1), none(n, 0);
     std::vector<double> rr, ff, rr_prev(n, -1), g0(n, 0), g1(n, 0);
+    std::vector<int> stalls(n, 0);
     std::vector<Scalars> res;
     if (p.precision == CFEM_FP32) {
       k_convert<double, float><<<nblk(c->nvec), kThreads, 0, c->stream>>>(c->nvec, c->v64.f.p, c->v32.f.p);
@@ -324,10 +325,11 @@ extern "C" cfem_status cfem_batch_static_solve(cfem_ctx *ctx, const cfem_solve_p
           act[i] = 0;
           if (status[i] == CFEM_OK || status[i] == CFEM_ERR_DIVERGED) continue;
           const bool conv = std::sqrt(rr[i]) <= outer_tol * std::sqrt(ff[i]);
-          // the FP64 true residual has a floor near eps64 * ||K|| ||x||: a
-          // refinement step that no longer reduces it as a step should ends
-          // the instance
-          const bool stalled = rr_prev[i] >= 0 && rr[i] > refine_stall_ratio(p.tol) * rr_prev[i];
+          // the FP64 true residual has a floor near eps64 * ||K|| ||x||: two
+          // refinement steps in a row that no longer reduce it as a step
+          // should end the instance
+          stalls[i] = rr_prev[i] >= 0 && rr[i] > refine_stall_ratio(p.tol) * rr_prev[i] ? stalls[i] + 1 : 0;
+          const bool stalled = stalls[i] >= 2;
           if (conv || stalled || ff[i] == 0.0) { status[i] = CFEM_OK; continue; }
           if (round == max_outer) continue;
           act[i] = 1;

@@ -310,6 +310,7 @@ cfem_status solve_batch(cfem_ctx *c, const cfem_solve_params &p, int kb, const d
   CK(cudaEventRecord(c->ev0, c->stream));
   std::vector<int> iters(kb, 0), outer(kb, 0), status(kb, CFEM_ERR_NOT_CONVERGED);
   std::vector<double> gamma0(kb, 0), gamma(kb, 0), rr(kb, 0), ff(kb, 0), rr_prev(kb, -1);
+  std::vector<int> stalls(kb, 0);
   std::vector<double> norms(2 * (size_t)kb, 0.0);
   auto residuals = [&](bool all) {
     // r_c = f_c - K' x_c in FP64 with ||r_c||^2 and ||f_c||^2 for the cases
@@ -365,9 +366,11 @@ cfem_status solve_batch(cfem_ctx *c, const cfem_solve_params &p, int kb, const d
         act[cs] = 0;
         if (status[cs] == CFEM_OK || status[cs] == CFEM_ERR_DIVERGED) continue;
         const bool conv = std::sqrt(rr[cs]) <= outer_tol * std::sqrt(ff[cs]);
-        // the FP64 true residual has a floor near eps64 * ||K|| ||x||: a
-        // refinement step that no longer halves it ends the case
-        const bool stalled = rr_prev[cs] >= 0 && rr[cs] > stall * rr_prev[cs];
+        // the FP64 true residual has a floor near eps64 * ||K|| ||x||: two
+        // refinement steps in a row that no longer reduce it as a step should
+        // end the case
+        stalls[cs] = rr_prev[cs] >= 0 && rr[cs] > stall * rr_prev[cs] ? stalls[cs] + 1 : 0;
+        const bool stalled = stalls[cs] >= 2;
         if (conv || stalled || ff[cs] == 0.0) { status[cs] = CFEM_OK; continue; }
         if (round == max_outer) continue;
         act[cs] = 1;
