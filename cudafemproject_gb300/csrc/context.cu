@@ -77,7 +77,10 @@ void launch_mv_t(cfem_ctx *c, int mode, const MvParams<T> &P) {
         return;
       }
       dim3 g(c->grid_ft32), b(kHfanThreads);
-      if (P.mcoef && mode == MV_PLAIN)
+      if (P.patch_inst) {
+        if (mode != MV_PCG || P.mcoef) throw Fail{CFEM_ERR_UNSUPPORTED, "batched meshes: PCG-form static matvec only"};
+        launch_pdl(k_matvec_fan_tma<float, MV_PCG, false, false, true>, g, b, c->smem_ft32, c->stream, P, F);
+      } else if (P.mcoef && mode == MV_PLAIN)
         k_matvec_fan_tma<float, MV_PLAIN, false, true><<<g, b, c->smem_ft32, c->stream>>>(P, F);
       else if (P.mcoef && mode == MV_PCG)
         launch_pdl(k_matvec_fan_tma<float, MV_PCG, false, true>, g, b, c->smem_ft32, c->stream, P, F);
@@ -842,7 +845,8 @@ void setup_context(cfem_ctx *c, const cfem_mesh *m, const cfem_material *mat, co
       for (const void *k : {(const void *)k_matvec_fan_tma<float, MV_PLAIN>, (const void *)k_matvec_fan_tma<float, MV_PCG>,
                             (const void *)k_matvec_fan_tma<float, MV_DYN>,
                             (const void *)k_matvec_fan_tma<float, MV_PLAIN, false, true>,
-                            (const void *)k_matvec_fan_tma<float, MV_PCG, false, true>})
+                            (const void *)k_matvec_fan_tma<float, MV_PCG, false, true>,
+                            (const void *)k_matvec_fan_tma<float, MV_PCG, false, false, true>})
         CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin - 8192));
       int o32 = 1;
       CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o32, k_matvec_fan_tma<float, MV_PCG>, kHfanThreads, c->smem_ft32));

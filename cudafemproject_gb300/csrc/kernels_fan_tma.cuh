@@ -197,9 +197,10 @@ struct FanTmaParams {
 };
 
 // MASS: the instance for operators with a consistent mass term (P.mcoef set;
-// implicit dynamics), kept apart so that the static instance carries none of
-// its registers.
-template <typename T, int MODE, bool GEO = false, bool MASS = false>
+// implicit dynamics); BATCH: the instance for batched independent meshes
+// (P.patch_inst set). Both are kept apart so that the single-mesh static
+// instance carries none of their registers.
+template <typename T, int MODE, bool GEO = false, bool MASS = false, bool BATCH = false>
 // (3 CTAs per SM: the shared memory of a CTA allows 3, the register bound makes them fit)
 __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> P, FanTmaParams F) {
   static_assert(sizeof(T) == 4, "patch blocks are FP32");
@@ -217,7 +218,7 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
   // by cp.async while the current one finishes, so their latency is hidden
   constexpr bool PREFETCH = GEO && MODE == MV_PCG;
   const int stage_stride = 2 * L.npn * VW;
-  const bool batch = P.patch_inst != nullptr;
+  constexpr bool batch = BATCH;
   const long long lim = F.wait_limit > 0 ? F.wait_limit : kWaitCycles;
   T lam = P.lam, mu = P.mu;
   __shared__ unsigned warps_done[2];  // warps finished with buffer 0 / 1 (see the end of the patch loop)
@@ -316,7 +317,7 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
           mbar_wait_bounded(&bar[b ^ 1], (phase >> (b ^ 1)) & 1u, lim);
       }
     };
-    if (batch && __syncthreads_or(!ok)) {  // (uniform: batch is a kernel parameter)
+    if (batch && __syncthreads_or(!ok)) {  // (uniform: batch is a template parameter)
       copy_failed();
       return;
     }
