@@ -129,7 +129,9 @@ typedef struct cfem_solve_params {
                             direction across the FP64 true-residual replacements (fastest near 0.3-0.4),
                             below 0.2 each step restarts it */
   int32_t max_iter;      /* PCG iteration cap (per inner solve) */
-  double outer_tol;      /* CFEM_FP32_REFINE: stop when ||f - K x||_2 <= outer_tol ||f||_2 */
+  double outer_tol;      /* CFEM_FP32_REFINE: stop when ||f - K x||_2 <= outer_tol ||f||_2, or (for an
+                            outer_tol below what FP64 can reach) when two refinement steps in a row no
+                            longer reduce the FP64 true residual; info.rel_residual reports where it ended */
   int32_t max_outer;     /* CFEM_FP32_REFINE: refinement step cap */
 } cfem_solve_params;
 
