@@ -297,7 +297,7 @@ def test_autotune_patch_elems():
 
 
 
-@pytest.mark.parametrize("loop", ["device", "host"])
+@pytest.mark.parametrize("loop", ["device", "host", "device_chunk6"])
 @pytest.mark.parametrize("precision", ["fp32", "fp64"])
 def test_pcg_termination_3d(precision, loop, monkeypatch):
     """Stopping paths of the 3D PCG (bulk-copy FP32 fan matvec, FP64 fan
@@ -307,13 +307,19 @@ def test_pcg_termination_3d(precision, loop, monkeypatch):
     exactly that count, on the same iterate as the oracle's PCG after as many
     steps (so every alpha and beta of the recurrence agrees). Both loops: the
     graph WHILE node (default) and the host relaunching 16-iteration graphs
-    (CFEM_HOST_LOOP, read when the context is created)."""
+    (CFEM_HOST_LOOP, read when the context is created); and the WHILE node with
+    6-iteration bodies (CFEM_PCG_CHUNK), so the caps fall inside, at the end of
+    and past a body."""
     from cudafemproject_gb300 import capi
     from cudafemproject_gb300.solver import FemContext
     if loop == "host":
         monkeypatch.setenv("CFEM_HOST_LOOP", "1")
     else:
         monkeypatch.delenv("CFEM_HOST_LOOP", raising=False)
+    if loop == "device_chunk6":
+        monkeypatch.setenv("CFEM_PCG_CHUNK", "6")
+    else:
+        monkeypatch.delenv("CFEM_PCG_CHUNK", raising=False)
     p = meshgen.box_3d(4, 4, 12, jitter=0.2, seed=4)
     o = O.Oracle(p, consistent=True)
     ctx = FemContext(p, semantics="consistent")
@@ -321,7 +327,7 @@ def test_pcg_termination_3d(precision, loop, monkeypatch):
     assert info["status"] == 0 and info["iterations"] == 0 and np.all(u == 0.0)
     f = o.rhs()
     tol = 1e-10 if precision == "fp64" else 2e-4
-    for m in (1, 2, 16, 17):
+    for m in (1, 2, 6, 12, 16, 17):
         u, info = ctx.pcg(f, precision, tol=1e-30, stop_rule="residual", max_iter=m, allow_not_converged=True)
         assert info["status"] == capi.ERR_NOT_CONVERGED and info["iterations"] == m, (m, info)
         x, its = o.pcg(f, tol=1e-30, rule=1, maxit=m, allow_maxit=True)
