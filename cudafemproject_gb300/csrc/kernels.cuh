@@ -40,13 +40,13 @@ struct Scalars {
   int rule, maxit, iter, done;  // done: 0 running, 1 converged, 2 diverged, 3 iteration cap
   unsigned int count_spare, count_up;  // count_up: grid-sum ticket of the init kernel
   int u_iter;  // iterations completed when the last update ran (-1: none since the init kernel)
-  int loops;   // device-side loop: bodies started in this run (pcg_matvec_scalars)
+  int loops;   // device-side loop: graph bodies started in this run (k_pcg_update)
   // alpha = gamma / sigma (set by CTA 0 of the update from the matvec's block
   // partials), beta = gamma / gamma_prev (set by CTA 0 of the matvec from the
   // update's block partials, 0 before the first direction): every CTA derives
   // them identically, so no thread divides differently
   double alpha, beta;
-  int loop_ok, pad2;  // device-side loop: loops within the cap
+  int loop_ok, pad2;  // device-side loop: the body count is within the cap (k_pcg_update)
 };
 
 struct DynState {
@@ -376,7 +376,6 @@ __device__ __forceinline__ double partials_total(const double *red, int k) {
 // loads, and shares the result through red (24 doubles of shared scratch):
 // the CTAs of a grid reading the same line thread by thread would queue at
 // one L2 slice.
-
 template <typename T>
 __device__ __forceinline__ bool pcg_matvec_scalars(Scalars *s, const double *up_part, int n_up, T &beta,
                                                    double *red) {
