@@ -1,8 +1,10 @@
 // sm_103a kernels of the element-by-element (EbE) elasticity path.
 //
 // Data layout in HBM (all in the locality order built by prep.cpp):
-//  * node vectors: VW values per node (VW = 4 in 3D, 2 in 2D; the pad lane is
-//    kept at zero) so that a node is one 16-byte (FP32) or 32-byte (FP64) load;
+//  * node vectors: VW values per node (VW = 4 in 3D, 2 in 2D) so that a node is
+//    one 16-byte (FP32) or 32-byte (FP64) load; the 3D pad lane is zero, except
+//    in the PCG's x, r, z and p, where it carries the Jacobi inverse of one DOF
+//    (k_pcg_init); kernels read the DOF lanes only;
 //  * element operator, gradient form: G = sqrt(V * E_e/E) * grad N_a for the
 //    local nodes a = 1..dim (N_0 follows from the partition of unity), stored
 //    structure-of-arrays [ncomp][gstride] so a warp reads 128 coalesced bytes
