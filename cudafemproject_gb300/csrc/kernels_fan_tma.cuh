@@ -303,6 +303,10 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
     // Every thread waits for the block itself; the staging barrier below
     // makes a failed copy a uniform exit (a thread whose wait failed reads
     // nothing of the block before it).
+    // the kernel after this one (launched with programmatic dependent launch)
+    // may start once every CTA is on its last patch: its CTAs take the SMs of
+    // the CTAs that finish early and wait there for this grid to complete
+    if (patch + step >= P.n_patches) griddep_launch_dependents();
     const bool live = patch_live(patch);
     bool ok = true;
     if (live) {
@@ -613,7 +617,6 @@ __global__ void __launch_bounds__(kHfanThreads, 3) k_matvec_fan_tma(MvParams<T> 
       }
     }
   }
-  griddep_launch_dependents();
   if (MODE == MV_PCG && !batch) {  // p.Ap partials; the update kernel forms sigma and alpha
     // (every warp is past the last patch's compute phase: the staging area is free)
     const DotAcc<T> ea[1] = {energy};
