@@ -119,7 +119,7 @@ def _host_cores() -> int:
 
 def _oracle():
     sys.path.insert(0, os.path.join(REPO, "oracle"))
-    import oracle  # the checker / CPU baseline only
+    import oracle  # the oracle: accuracy reference and CPU baseline only
     return oracle
 
 

@@ -2,7 +2,7 @@
  * fem_oracle.c -- TEST INFRASTRUCTURE ONLY (see fem_oracle.h).
  *
  * CPU restatement of the reference's EbE elasticity path. Used by tests/ as
- * the checker and by bench.py's cpu_baseline leg; never by the product.
+ * the parity reference and by bench.py's cpu_baseline leg; never by the product.
  */
 #include "fem_oracle.h"
 

@@ -2,7 +2,7 @@
  * fem_oracle.h -- TEST INFRASTRUCTURE ONLY.
  *
  * CPU restatement of the reference's element-by-element (EbE) linear
- * elasticity path (moarseniy/CudaFEMproject), used by tests/ as the checker,
+ * elasticity path (moarseniy/CudaFEMproject), used by tests/ as the parity reference,
  * by __graft_entry__.smoke() and by bench.py's cpu_baseline leg. The product
  * (cudafemproject_gb300) never links, loads or calls this code.
  *

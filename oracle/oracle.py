@@ -1,7 +1,7 @@
 """TEST INFRASTRUCTURE ONLY: ctypes view of the C oracle (oracle/fem_oracle.c).
 
 Imported by tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg,
-always as the checker / CPU baseline, never as the product path.
+always as the parity reference / CPU baseline, never as the product path.
 """
 from __future__ import annotations
 
